@@ -1,0 +1,495 @@
+// hc_api.cu -- the extern "C" entry points declared in include/hydrocuda.h.
+#include "hc_internal.h"
+
+#include <cmath>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace hc {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return e == cudaErrorMemoryAllocation ? HC_ERR_NOMEM : HC_ERR_CUDA;
+}
+
+}  // namespace hc
+
+using namespace hc;
+
+struct hc_context {
+    int device;
+    cudaStream_t stream;
+};
+
+struct hc_solver {
+    hc_context* ctx;
+    hc_solver_desc d;
+    PlainSolver* plain = nullptr;
+    FusedSet* fused = nullptr;
+    double t = 0;           // plain form: SolverBase.t (a Lua double in the reference)
+    long long steps = 0;
+};
+
+struct hc_batch {
+    hc_context* ctx;
+    hc_batch_desc d;
+    FusedSet* fused = nullptr;
+    size_t bytes_in_use = 0;
+    std::vector<size_t> slot_bytes;
+    std::vector<unsigned long long> tags;
+    std::vector<char> used, reported;
+};
+
+namespace {
+
+int use_device(const hc_context* ctx) {
+    HC_CUDA(cudaSetDevice(ctx->device));
+    return HC_OK;
+}
+
+int validate_desc(const hc_solver_desc* d) {
+    if (!d) return fail(HC_ERR_INVALID, "descriptor is NULL");
+    if (d->dim < 1 || d->dim > 3) return fail(HC_ERR_INVALID, "dim must be 1, 2 or 3");
+    for (int k = 0; k < d->dim; ++k) {
+        if (d->n[k] < 2) return fail(HC_ERR_INVALID, "gridSize must be at least 2 on each active axis");
+        if (!(d->maxs[k] > d->mins[k])) return fail(HC_ERR_INVALID, "maxs must exceed mins");
+    }
+    for (int k = 0; k < 6; ++k)
+        if (d->boundary[k] < HC_BOUNDARY_NONE || d->boundary[k] > HC_BOUNDARY_FREEFLOW)
+            return fail(HC_ERR_INVALID, "unknown boundary");
+    if (d->flux_limiter < 0 || d->flux_limiter >= HC_NUM_LIMITERS) return fail(HC_ERR_INVALID, "unknown flux limiter");
+    if (d->slope_limiter < 0 || d->slope_limiter >= HC_NUM_LIMITERS) return fail(HC_ERR_INVALID, "unknown slope limiter");
+    if (d->recon < HC_RECON_NONE || d->recon > HC_RECON_PLM_CONS) return fail(HC_ERR_INVALID, "unknown usePLM");
+    if (d->recon != HC_RECON_NONE && d->flux_limiter > 0)
+        return fail(HC_ERR_INVALID, "usePLM together with a flux limiter (gridsolver.lua:119 asserts against it)");
+    if (d->integrator < 0 || d->integrator >= HC_NUM_INTEGRATORS) return fail(HC_ERR_INVALID, "unknown integrator");
+    if (d->precision < HC_F64_PLAIN || d->precision > HC_F32_FUSED) return fail(HC_ERR_INVALID, "unknown precision");
+    if (!(d->gamma > 1.)) return fail(HC_ERR_INVALID, "gamma must exceed 1");
+    if (!(d->cfl > 0.) && !(d->fixed_dt > 0.)) return fail(HC_ERR_INVALID, "cfl must be positive");
+    return HC_OK;
+}
+
+long long interior_cells(const hc_solver_desc& d) {
+    long long n = 1;
+    for (int k = 0; k < d.dim; ++k) n *= d.n[k];
+    return n;
+}
+
+FusedScheme scheme_of(const hc_solver_desc& d) {
+    FusedScheme s;
+    s.precision = d.precision;
+    s.flux_limiter = d.flux_limiter;
+    s.recon = d.recon;
+    s.slope_limiter = d.slope_limiter;
+    s.integrator = d.integrator;
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hc_version(void) { return "0.3"; }
+
+const char* hc_last_error(void) { return g_last_error.c_str(); }
+
+int hc_device_count(int* count) {
+    if (!count) return fail(HC_ERR_INVALID, "count is NULL");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) { *count = 0; return cuda_fail(e, "cudaGetDeviceCount"); }
+    *count = n;
+    return HC_OK;
+}
+
+int hc_context_create(int device, hc_context** out) {
+    if (!out) return fail(HC_ERR_INVALID, "out is NULL");
+    int n = 0;
+    HC_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(HC_ERR_INVALID, "no such device");
+    HC_CUDA(cudaSetDevice(device));
+    hc_context* c = new hc_context();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
+    *out = c;
+    return HC_OK;
+}
+
+int hc_context_destroy(hc_context* ctx) {
+    if (!ctx) return HC_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return HC_OK;
+}
+
+int hc_host_alloc(size_t bytes, void** out) {
+    if (!out) return fail(HC_ERR_INVALID, "out is NULL");
+    HC_CUDA(cudaMallocHost(out, bytes));
+    return HC_OK;
+}
+
+int hc_host_free(void* p) {
+    if (p) HC_CUDA(cudaFreeHost(p));
+    return HC_OK;
+}
+
+// ---- solver ---------------------------------------------------------------
+
+int hc_solver_create(hc_context* ctx, const hc_solver_desc* desc, hc_solver** out) {
+    if (!ctx || !out) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(validate_desc(desc));
+    HC_CHECK(use_device(ctx));
+    hc_solver* s = new hc_solver();
+    s->ctx = ctx;
+    s->d = *desc;
+    int r;
+    if (desc->precision == HC_F64_PLAIN) {
+        r = plain_create(*desc, ctx->stream, &s->plain);
+    } else {
+        r = fused_create(scheme_of(*desc), 1, ctx->stream, &s->fused);
+        if (r == HC_OK) r = fused_add(s->fused, 0, *desc, nullptr, HC_LAYOUT_AOS6_F64, INFINITY, LLONG_MAX);
+    }
+    if (r != HC_OK) {
+        std::string const msg = g_last_error;
+        hc_solver_destroy(s);
+        g_last_error = msg;
+        return r;
+    }
+    *out = s;
+    return HC_OK;
+}
+
+int hc_solver_destroy(hc_solver* s) {
+    if (!s) return HC_OK;
+    cudaSetDevice(s->ctx->device);
+    if (s->plain) plain_destroy(s->plain);
+    if (s->fused) fused_destroy(s->fused);
+    delete s;
+    return HC_OK;
+}
+
+int hc_solver_reset_state(hc_solver* s, const void* cons, int layout) {
+    if (!s || !cons) return fail(HC_ERR_INVALID, "NULL argument");
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    HC_CHECK(use_device(s->ctx));
+    if (s->plain) {
+        HC_CHECK(plain_set_interior(s->plain, cons, layout));
+        HC_CHECK(plain_boundary(s->plain));
+        HC_CHECK(plain_constrain_u(s->plain));
+        s->t = 0;
+        s->steps = 0;
+        HC_CUDA(cudaStreamSynchronize(s->ctx->stream));
+        return HC_OK;
+    }
+    HC_CHECK(fused_set_state(s->fused, 0, cons, layout, 1));
+    HC_CHECK(fused_set_time(s->fused, 0, 0.));
+    return fused_sync(s->fused);
+}
+
+int hc_solver_set_state(hc_solver* s, const void* cons, int layout, int with_ghosts) {
+    if (!s || !cons) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(s->ctx));
+    if (with_ghosts) {
+        if (!s->plain || layout != HC_LAYOUT_AOS6_F64) return fail(HC_ERR_INVALID, "ghost-inclusive state I/O is AOS6_F64 on the plain form only");
+        return plain_set_full(s->plain, (const double*)cons);
+    }
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    if (s->plain) return plain_set_interior(s->plain, cons, layout);
+    HC_CHECK(fused_set_state(s->fused, 0, cons, layout, 0));
+    return fused_sync(s->fused);
+}
+
+int hc_solver_get_state(hc_solver* s, void* cons, int layout, int with_ghosts) {
+    if (!s || !cons) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(s->ctx));
+    if (with_ghosts) {
+        if (!s->plain || layout != HC_LAYOUT_AOS6_F64) return fail(HC_ERR_INVALID, "ghost-inclusive state I/O is AOS6_F64 on the plain form only");
+        return plain_get_full(s->plain, (double*)cons);
+    }
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    if (s->plain) return plain_get_interior(s->plain, cons, layout);
+    return fused_get_state(s->fused, 0, cons, layout);
+}
+
+int hc_solver_boundary(hc_solver* s) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    HC_CHECK(use_device(s->ctx));
+    if (s->plain) HC_CHECK(plain_boundary(s->plain));
+    else HC_CHECK(fused_boundary(s->fused, 0));
+    HC_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return HC_OK;
+}
+
+int hc_solver_constrain_u(hc_solver* s) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    HC_CHECK(use_device(s->ctx));
+    if (s->plain) HC_CHECK(plain_constrain_u(s->plain));
+    else HC_CHECK(fused_constrain_u(s->fused, 0));
+    HC_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return HC_OK;
+}
+
+int hc_solver_calc_dt(hc_solver* s, double* dt) {
+    if (!s || !dt) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(s->ctx));
+    if (s->plain) return plain_calc_dt(s->plain, s->d.cfl, s->d.fixed_dt, dt);
+    return fused_calc_dt(s->fused, 0, dt);
+}
+
+int hc_solver_step(hc_solver* s, double dt) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    if (!(dt >= 0) || !std::isfinite(dt)) return fail(HC_ERR_INVALID, "dt must be finite and non-negative");
+    HC_CHECK(use_device(s->ctx));
+    if (s->plain) {
+        HC_CHECK(plain_step(s->plain, s->d.integrator, dt));
+        HC_CUDA(cudaStreamSynchronize(s->ctx->stream));
+        return HC_OK;
+    }
+    HC_CHECK(fused_step_dt(s->fused, 0, dt));
+    return fused_sync(s->fused);
+}
+
+static int solver_status(hc_solver* s) {
+    if (s->plain) return HC_OK;
+    std::vector<SlotInfo> info;
+    HC_CHECK(fused_slot_info(s->fused, info));
+    if (info[0].status & DEV_TIMEOUT) return fail(HC_ERR_TIMEOUT, "a bounded device wait ran out");
+    if (info[0].status & DEV_NONFINITE) return fail(HC_ERR_NONFINITE, "the solve produced a non-finite state or dt");
+    return HC_OK;
+}
+
+int hc_solver_update(hc_solver* s, double* dt_out) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    HC_CHECK(use_device(s->ctx));
+    if (s->plain) {
+        double dt;
+        HC_CHECK(plain_calc_dt(s->plain, s->d.cfl, s->d.fixed_dt, &dt));
+        if (!std::isfinite(dt)) return fail(HC_ERR_NONFINITE, "calcDT produced a non-finite dt");
+        HC_CHECK(plain_step(s->plain, s->d.integrator, dt));
+        s->t = s->t + dt;
+        s->steps += 1;
+        HC_CHECK(plain_boundary(s->plain));
+        HC_CUDA(cudaStreamSynchronize(s->ctx->stream));
+        if (dt_out) *dt_out = dt;
+        return HC_OK;
+    }
+    std::vector<SlotInfo> info;
+    HC_CHECK(fused_slot_info(s->fused, info));
+    HC_CHECK(fused_set_limits(s->fused, 0, INFINITY, info[0].steps + 1));
+    HC_CHECK(fused_steps(s->fused, 1));
+    HC_CHECK(fused_sync(s->fused));
+    HC_CHECK(fused_slot_info(s->fused, info));
+    if (dt_out) *dt_out = info[0].dt;
+    return solver_status(s);
+}
+
+int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long long* steps_done) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    if (max_steps < 0) return fail(HC_ERR_INVALID, "max_steps");
+    HC_CHECK(use_device(s->ctx));
+    long long n = 0;
+    if (s->plain) {
+        while (!(s->t >= t_end) && n < max_steps) {
+            HC_CHECK(hc_solver_update(s, nullptr));
+            ++n;
+        }
+        if (steps_done) *steps_done = n;
+        return HC_OK;
+    }
+    std::vector<SlotInfo> info;
+    HC_CHECK(fused_slot_info(s->fused, info));
+    long long const start = info[0].steps;
+    long long const limit = max_steps > LLONG_MAX - start ? LLONG_MAX : start + max_steps;
+    HC_CHECK(fused_set_limits(s->fused, 0, t_end, limit));
+    int chunk = 4;
+    for (;;) {
+        HC_CHECK(fused_steps(s->fused, chunk));
+        HC_CHECK(fused_sync(s->fused));
+        HC_CHECK(fused_slot_info(s->fused, info));
+        if (!info[0].active || info[0].done) break;
+        if (chunk < 64) chunk *= 2;
+    }
+    if (steps_done) *steps_done = info[0].steps - start;
+    return solver_status(s);
+}
+
+int hc_solver_get_time(hc_solver* s, double* t) {
+    if (!s || !t) return fail(HC_ERR_INVALID, "NULL argument");
+    if (s->plain) { *t = s->t; return HC_OK; }
+    HC_CHECK(use_device(s->ctx));
+    std::vector<SlotInfo> info;
+    HC_CHECK(fused_slot_info(s->fused, info));
+    *t = info[0].t;
+    return HC_OK;
+}
+
+int hc_solver_set_time(hc_solver* s, double t) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    if (s->plain) { s->t = t; return HC_OK; }
+    HC_CHECK(use_device(s->ctx));
+    return fused_set_time(s->fused, 0, t);
+}
+
+int hc_solver_conservation(hc_solver* s, double sums[5]) {
+    if (!s || !sums) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(s->ctx));
+    if (s->plain) return plain_conservation(s->plain, sums);
+    return fused_conservation(s->fused, 0, sums);
+}
+
+int hc_solver_status(hc_solver* s) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    HC_CHECK(use_device(s->ctx));
+    return solver_status(s);
+}
+
+// ---- batch ------------------------------------------------------------------
+
+int hc_batch_create(hc_context* ctx, const hc_batch_desc* desc, hc_batch** out) {
+    if (!ctx || !desc || !out) return fail(HC_ERR_INVALID, "NULL argument");
+    if (desc->precision != HC_F32_FUSED && desc->precision != HC_F64_FUSED)
+        return fail(HC_ERR_INVALID, "a batch runs the fused form (HC_F32_FUSED or HC_F64_FUSED)");
+    if (desc->max_slots <= 0 || desc->max_slots > (1 << 20)) return fail(HC_ERR_INVALID, "max_slots");
+    HC_CHECK(use_device(ctx));
+    FusedScheme sch;
+    sch.precision = desc->precision;
+    sch.flux_limiter = desc->flux_limiter;
+    sch.recon = desc->recon;
+    sch.slope_limiter = desc->slope_limiter;
+    sch.integrator = desc->integrator;
+    hc_batch* b = new hc_batch();
+    b->ctx = ctx;
+    b->d = *desc;
+    int const r = fused_create(sch, desc->max_slots, ctx->stream, &b->fused);
+    if (r != HC_OK) { delete b; return r; }
+    b->slot_bytes.assign(desc->max_slots, 0);
+    b->tags.assign(desc->max_slots, 0);
+    b->used.assign(desc->max_slots, 0);
+    b->reported.assign(desc->max_slots, 0);
+    *out = b;
+    return HC_OK;
+}
+
+int hc_batch_destroy(hc_batch* b) {
+    if (!b) return HC_OK;
+    cudaSetDevice(b->ctx->device);
+    fused_destroy(b->fused);
+    delete b;
+    return HC_OK;
+}
+
+int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout,
+                   double t_end, long long max_steps, unsigned long long tag, int* slot) {
+    if (!b || !desc || !cons || !slot) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(validate_desc(desc));
+    if (desc->recon != b->d.recon || desc->slope_limiter != b->d.slope_limiter || desc->flux_limiter != b->d.flux_limiter ||
+        desc->integrator != b->d.integrator)
+        return fail(HC_ERR_INVALID, "the instance's scheme differs from the batch's");
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    if (max_steps <= 0) max_steps = LLONG_MAX;
+    HC_CHECK(use_device(b->ctx));
+    size_t const bytes = fused_instance_bytes(b->fused, *desc);
+    if (b->bytes_in_use + bytes > b->d.hbm_budget)
+        return fail(HC_ERR_BUDGET, "admission would exceed the batch's HBM budget");
+    int s = -1;
+    for (int k = 0; k < b->d.max_slots; ++k)
+        if (!b->used[k]) { s = k; break; }
+    if (s < 0) return fail(HC_ERR_NO_SLOT, "every slot is in use");
+    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps));
+    b->used[s] = 1;
+    b->reported[s] = 0;
+    b->tags[s] = tag;
+    b->slot_bytes[s] = bytes;
+    b->bytes_in_use += bytes;
+    *slot = s;
+    return HC_OK;
+}
+
+int hc_batch_step(hc_batch* b, int steps, int* n_active) {
+    if (!b) return fail(HC_ERR_INVALID, "NULL batch");
+    HC_CHECK(use_device(b->ctx));
+    HC_CHECK(fused_steps(b->fused, steps));
+    HC_CHECK(fused_sync(b->fused));
+    if (n_active) {
+        std::vector<SlotInfo> info;
+        HC_CHECK(fused_slot_info(b->fused, info));
+        int n = 0;
+        for (int k = 0; k < b->d.max_slots; ++k) n += b->used[k] && info[k].active;
+        *n_active = n;
+    }
+    return HC_OK;
+}
+
+int hc_batch_poll(hc_batch* b, hc_done* out, int cap, int* n_out) {
+    if (!b || !n_out || (cap > 0 && !out)) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(b->ctx));
+    std::vector<SlotInfo> info;
+    HC_CHECK(fused_slot_info(b->fused, info));
+    int n = 0;
+    for (int k = 0; k < b->d.max_slots && n < cap; ++k) {
+        if (!b->used[k] || b->reported[k] || !info[k].done) continue;
+        out[n].slot = k;
+        out[n].status = info[k].status ? (info[k].status & DEV_TIMEOUT ? HC_ERR_TIMEOUT : HC_ERR_NONFINITE) : HC_OK;
+        out[n].tag = b->tags[k];
+        out[n].steps = info[k].steps;
+        out[n].t = info[k].t;
+        b->reported[k] = 1;
+        ++n;
+    }
+    *n_out = n;
+    return HC_OK;
+}
+
+int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout) {
+    if (!b || !cons) return fail(HC_ERR_INVALID, "NULL argument");
+    if (slot < 0 || slot >= b->d.max_slots || !b->used[slot]) return fail(HC_ERR_STATE, "slot not in use");
+    HC_CHECK(use_device(b->ctx));
+    return fused_get_state(b->fused, slot, cons, layout);
+}
+
+int hc_batch_retire(hc_batch* b, int slot) {
+    if (!b) return fail(HC_ERR_INVALID, "NULL batch");
+    if (slot < 0 || slot >= b->d.max_slots || !b->used[slot]) return fail(HC_ERR_STATE, "slot not in use");
+    HC_CHECK(use_device(b->ctx));
+    HC_CHECK(fused_remove(b->fused, slot));
+    b->used[slot] = 0;
+    b->bytes_in_use -= b->slot_bytes[slot];
+    b->slot_bytes[slot] = 0;
+    return HC_OK;
+}
+
+int hc_batch_stats_get(hc_batch* b, hc_batch_stats* st) {
+    if (!b || !st) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(b->ctx));
+    return fused_stats(b->fused, st);
+}
+
+int hc_batch_conservation(hc_batch* b, int slot, double sums[5]) {
+    if (!b || !sums) return fail(HC_ERR_INVALID, "NULL argument");
+    if (slot < 0 || slot >= b->d.max_slots || !b->used[slot]) return fail(HC_ERR_STATE, "slot not in use");
+    HC_CHECK(use_device(b->ctx));
+    return fused_conservation(b->fused, slot, sums);
+}
+
+int hc_batch_autotune(hc_batch* b, const char* cache_path) {
+    if (!b) return fail(HC_ERR_INVALID, "NULL batch");
+    HC_CHECK(use_device(b->ctx));
+    return fused_autotune(b->fused, cache_path);
+}
+
+}  // extern "C"

@@ -1,0 +1,243 @@
+// hc_fast_math.cuh -- the same Euler / Roe / PLM arithmetic as hc_ref_math.cuh,
+// restated in the frame of the interface normal for throughput.
+//
+// With hydro-cl-lua's Cartesian side-permutation normals
+// (hydro/coord/coord.lua:2341-2409) the reference's 5x5 left/right eigenvector
+// transforms (hydro/eqn/euler.cl:434-542) contain only 0/1 normal components.
+// Expressed in the rotated frame (n, t1, t2) = (side, side+1, side+2) they
+// reduce to a handful of shared sub-expressions:
+//
+//   L.X:  q = (g-1)(X0 vSq/2 - X_m.v + X4),  k = Cs (X0 vn - Xn),
+//         w0 = (q + k)/(2Cs^2), w1 = X0 - 2q/(2Cs^2), w2 = Xt1 - X0 vt1,
+//         w3 = Xt2 - X0 vt2,   w4 = (q - k)/(2Cs^2)
+//   R.W:  S = W0 + W1 + W4,  D = W4 - W0
+//         F = (S, S vn + Cs D, S vt1 + W2, S vt2 + W3,
+//              hT (W0 + W4) + Cs vn D + vSq W1/2 + vt1 W2 + vt2 W3)
+//
+// which is algebraically identical to the reference; only rounding differs.
+// Branches (vacuum states, rhoMin / PMin guards, the limiter selectors) are
+// kept exactly.  Single precision uses the fast reciprocal / square-root
+// intrinsics; the FP32 form is held to the density L1 tolerance against the
+// FP64 oracle, not to bitwise parity.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace hc {
+namespace fast {
+
+template <typename T> struct M;
+template <> struct M<float> {
+    static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.f, x); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
+};
+template <> struct M<double> {
+    static __device__ __forceinline__ double rcp(double x) { return 1. / x; }
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double inf() { return __longlong_as_double(0x7ff0000000000000ll); }
+};
+
+template <typename T> __device__ __forceinline__ T tmax(T x, T y) { return x < y ? y : x; }
+template <typename T> __device__ __forceinline__ T tmin(T x, T y) { return y < x ? y : x; }
+
+// hydro/app.lua:614-635
+template <typename T>
+__device__ __forceinline__ T limiter(int which, T r) {
+    T const z = T(0), one = T(1), two = T(2);
+    switch (which) {
+    case 0: return z;
+    case 1: return one;
+    case 2: return r;
+    case 3: return T(.5) * (one + r);
+    case 4: return M<T>::div(tmax(z, r) * (T(3) * r + one), (r + one) * (r + one));
+    case 5: return tmax(z, M<T>::div(T(1.5) * (r + fabs(r)), r + two));
+    case 6: return tmax(z, M<T>::div(two * (r + fabs(r)), r + T(3)));
+    case 7: return tmax(z, tmin(two * r, tmin(M<T>::div(one + two * r, T(3)), two)));
+    case 8: return tmax(z, tmin(r, one));
+    case 9: return tmax(z, tmin(r, T(1.5)));
+    case 10: return M<T>::div(T(.5) * (r * r + r), r * r + r + one);
+    case 11: return tmax(z, tmin(two * r, tmin(T(.25) + T(.75) * r, T(4))));
+    case 12: return tmax(z, tmax(tmin(T(1.5) * r, one), tmin(r, T(1.5))));
+    case 13: return tmax(z, tmin(tmin(two * r, T(.75) + T(.25) * r), tmin(T(.25) + T(.75) * r, two)));
+    case 14: return M<T>::div(r * r + r, r * r + one);
+    case 15: return M<T>::div(two * r, r * r + one);
+    case 16: return M<T>::div(tmax(z, r) * two, one + r);
+    case 17: return tmax(z, tmin(two, tmin(T(.5) * (one + r), two * r)));
+    case 18: return tmax(z, tmax(tmin(one, two * r), tmin(two, r)));
+    case 19: return T(.5) * (r + one) * tmin(one, tmin(M<T>::div(T(4) * r, r + one), M<T>::div(T(4), r + one)));
+    }
+    return z;
+}
+
+template <typename T> struct Eos {
+    T gamma, g1, rhoMin, PMin;
+    int fluxLimiter, slopeLimiter;
+};
+
+// A conserved state in the interface frame: rho, m_n, m_t1, m_t2, ETotal.
+template <typename T> struct C5 { T u[5]; };
+
+// Roe eigen-state in the interface frame.  ident: the transforms are the
+// identity (eig.rho < rhoMin).
+template <typename T> struct EigF {
+    T vn, vt1, vt2, hT, Cs, vSq, invD;
+    bool ident;
+};
+
+// Primitive quantities used by the Roe average (euler.cl:140-159, 79-83).
+template <typename T>
+__device__ __forceinline__ void primOf(const C5<T>& U, const Eos<T>& s, T& inv, T& P) {
+    inv = M<T>::rcp(U.u[0]);
+    T const m2 = U.u[1] * U.u[1] + U.u[2] * U.u[2] + U.u[3] * U.u[3];
+    T const EKin = U.u[0] < s.rhoMin ? T(0) : T(.5) * m2 * inv;
+    P = U.u[0] < s.rhoMin ? T(0) : s.g1 * (U.u[4] - EKin);
+}
+
+// eigen_forInterface (euler.cl:347-430) in the interface frame.
+template <typename T>
+__device__ __forceinline__ void eigen(EigF<T>& e, const Eos<T>& s, const C5<T>& UL, const C5<T>& UR) {
+    T const eps = T(1e-5);
+    bool const lv = UL.u[0] < eps, rv = UR.u[0] < eps;
+    T rho;
+    if (lv && rv) {
+        rho = T(0);
+        e.vn = e.vt1 = e.vt2 = T(0);
+        e.vSq = T(0);
+        e.hT = T(0);
+        e.Cs = T(0);
+    } else if (lv || rv) {
+        const C5<T>& Uo = lv ? UR : UL;
+        T inv, P;
+        primOf(Uo, s, inv, P);
+        rho = Uo.u[0];
+        e.vn = Uo.u[1] * inv;
+        e.vt1 = Uo.u[2] * inv;
+        e.vt2 = Uo.u[3] * inv;
+        e.vSq = e.vn * e.vn + e.vt1 * e.vt1 + e.vt2 * e.vt2;
+        e.hT = (P + Uo.u[4]) * inv;
+        e.Cs = P <= s.PMin ? T(0) : (Uo.u[0] < s.rhoMin ? M<T>::inf() : M<T>::sqrt_(s.gamma * P * inv));
+    } else {
+        T invL, PL, invR, PR;
+        primOf(UL, s, invL, PL);
+        primOf(UR, s, invR, PR);
+        T const sL = M<T>::sqrt_(UL.u[0]);
+        T const sR = M<T>::sqrt_(UR.u[0]);
+        T const hTL = (PL + UL.u[4]) * invL;
+        T const hTR = (PR + UR.u[4]) * invR;
+        T const invDen = M<T>::rcp(sL + sR);
+        // sqrt(rhoL) * v_L = m_L / sqrt(rhoL)
+        T const aL = sL * invDen * invL, aR = sR * invDen * invR;
+        rho = sL * sR;
+        e.vn = UL.u[1] * aL + UR.u[1] * aR;
+        e.vt1 = UL.u[2] * aL + UR.u[2] * aR;
+        e.vt2 = UL.u[3] * aL + UR.u[3] * aR;
+        T const hT = invDen * (sL * hTL + sR * hTR);
+        e.vSq = e.vn * e.vn + e.vt1 * e.vt1 + e.vt2 * e.vt2;
+        T const eKin = T(.5) * e.vSq;
+        T const h = hT - eKin;
+        if (h < eps) {
+            e.hT = eKin;
+            e.Cs = T(0);
+        } else {
+            e.hT = hT;
+            e.Cs = M<T>::sqrt_(s.g1 * h);
+        }
+    }
+    e.ident = rho < s.rhoMin;
+    e.invD = M<T>::rcp(T(2) * e.Cs * e.Cs);
+}
+
+// eigen_leftTransform (euler.cl:434-489) in the interface frame.
+template <typename T>
+__device__ __forceinline__ void left(T* w, const EigF<T>& e, const Eos<T>& s, const T* X) {
+    if (e.ident) {
+        for (int j = 0; j < 5; ++j) w[j] = X[j];
+        return;
+    }
+    T const mv = X[1] * e.vn + X[2] * e.vt1 + X[3] * e.vt2;
+    T const q = s.g1 * (T(.5) * X[0] * e.vSq - mv + X[4]);
+    T const k = e.Cs * (X[0] * e.vn - X[1]);
+    w[0] = (q + k) * e.invD;
+    w[1] = X[0] - T(2) * q * e.invD;
+    w[2] = X[2] - X[0] * e.vt1;
+    w[3] = X[3] - X[0] * e.vt2;
+    w[4] = (q - k) * e.invD;
+}
+
+// eigen_rightTransform (euler.cl:493-542) in the interface frame.
+template <typename T>
+__device__ __forceinline__ void right(T* F, const EigF<T>& e, const T* W) {
+    if (e.ident) {
+        for (int j = 0; j < 5; ++j) F[j] = W[j];
+        return;
+    }
+    T const S = W[0] + W[1] + W[4];
+    T const D = W[4] - W[0];
+    T const CsD = e.Cs * D;
+    F[0] = S;
+    F[1] = S * e.vn + CsD;
+    F[2] = S * e.vt1 + W[2];
+    F[3] = S * e.vt2 + W[3];
+    F[4] = e.hT * (W[0] + W[4]) + e.vn * CsD + T(.5) * e.vSq * W[1] + e.vt1 * W[2] + e.vt2 * W[3];
+}
+
+// Interface data reused by the flux limiter of the neighbouring interfaces.
+template <typename T> struct IfaceF {
+    EigF<T> e;
+    T dW[5];
+};
+
+template <typename T>
+__device__ __forceinline__ void makeIface(IfaceF<T>& I, const Eos<T>& s, const C5<T>& UL, const C5<T>& UR) {
+    eigen(I.e, s, UL, UR);
+    T dU[5];
+    for (int j = 0; j < 5; ++j) dU[j] = UR.u[j] - UL.u[j];
+    left(I.dW, I.e, s, dU);
+}
+
+// Roe flux (roe.cl:17-163) at interface C; IL / IR are the neighbouring
+// interfaces (used only with the flux limiter).
+template <typename T, bool LIM>
+__device__ __forceinline__ void roe(T* F, const Eos<T>& s, const C5<T>& UL, const C5<T>& UR,
+                                    const IfaceF<T>& C, const IfaceF<T>& IL, const IfaceF<T>& IR, T dt_dx) {
+    T UA[5];
+    for (int j = 0; j < 5; ++j) UA[j] = T(.5) * (UL.u[j] + UR.u[j]);
+    T fe[5];
+    left(fe, C.e, s, UA);
+    T const vn = C.e.vn, Cs = C.e.Cs;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        T const lambda = j == 0 ? vn - Cs : (j == 4 ? vn + Cs : vn);
+        T const sgn = lambda >= T(0) ? T(1) : T(-1);
+        if (LIM) {
+            T rEig;
+            if (C.dW[j] == T(0)) rEig = T(0);
+            else rEig = M<T>::div(lambda >= T(0) ? IL.dW[j] : IR.dW[j], C.dW[j]);
+            T const phi = limiter<T>(s.fluxLimiter, rEig);
+            fe[j] = fe[j] * lambda - T(.5) * lambda * C.dW[j] * (sgn + phi * (lambda * dt_dx - sgn));
+        } else {
+            fe[j] = fe[j] * lambda - T(.5) * lambda * C.dW[j] * sgn;
+        }
+    }
+    right(F, C.e, fe);
+}
+
+// "plm cons" slope of one component: returns sigma.
+template <typename T>
+__device__ __forceinline__ T plmSigma(T um, T u0, T up, int lim) {
+    T const dUR = up - u0;
+    T const dUL = u0 - um;
+    T const dUC = T(.5) * (dUR - dUL);
+    bool const pos = dUC >= T(0);
+    T const num = pos ? dUL : dUR;
+    T const den = pos ? dUR : dUL;
+    T const r = den == T(0) ? T(0) : M<T>::div(num, den);
+    return limiter<T>(lim, r) * den;
+}
+
+}  // namespace fast
+}  // namespace hc

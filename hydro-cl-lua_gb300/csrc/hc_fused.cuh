@@ -1,0 +1,813 @@
+// hc_fused.cuh -- the fused stage kernel: one launch per Runge-Kutta stage
+// replaces the reference's boundary / calcLR / calcFlux / calcDerivFromFlux /
+// multAdd / constrainU / calcDT sequence for every tile of every instance.
+//
+// Layout in HBM: per instance and per state buffer, 5 structure-of-arrays
+// planes (rho, m.x, m.y, m.z, ETotal) of the padded grid (numGhost = 2 ghost
+// layers on each active axis, rows padded to 32 elements).  ePot is always 0
+// for these problems and is not stored.
+//
+// Per tile (TX x TY x TZ interior cells) a CTA:
+//   1. stages the tile plus its 2-cell halo (a (TX+4)(TY+4)(TZ+4) x 5 box)
+//      into shared memory with one TMA tensor load (cp.async.bulk.tensor,
+//      mbarrier completion, bounded wait);
+//   2. sweeps every axis but the last with one thread per line segment of L
+//      cells: a register window slides along the segment, computing each
+//      cell's PLM slope once and each interface's Roe flux once, and writes
+//      the flux difference of each cell into a shared-memory accumulator
+//      (calcDerivFromFlux: deriv = ((0 - X) - Y) - Z);
+//   3. sweeps the last axis the same way, and as each cell's last face flux
+//      is known, finishes the cell: Runge-Kutta combination
+//      (u = sum alpha_k u^(k) + dt sum beta_k L(u^(k)), terms in the
+//      reference's order), constrainU, the store, the ghost copies the
+//      boundary condition maps to this cell (the boundary fill becomes a
+//      scatter, so no separate boundary launch exists), and on the last stage
+//      the cell's CFL dt, reduced by warp shuffles into one FP64 atomicMin
+//      per warp.
+//
+// Two arithmetic forms share this code: EXACT (double, the reference's
+// literal expressions from hc_ref_math.cuh, compiled without FMA
+// contraction) and fast (hc_fast_math.cuh, any precision).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hc_internal.h"
+#include "hc_ref_math.cuh"
+#include "hc_fast_math.cuh"
+
+namespace hc {
+namespace fz {
+
+constexpr int kMaxBufs = 4;      // state buffers per instance
+constexpr int kMaxDBufs = 4;     // stored-derivative buffers per instance
+constexpr int kG = 2;            // numGhost
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
+
+struct DevInst {
+    int dim;
+    int n[3];              // interior extents (1 on unused axes)
+    int px, py, pz;        // padded extents; px is the row pitch in elements
+    long long plane;       // elements per field plane
+    int bc[6];
+    double grid_dx[3];
+    double area[3];        // areaL * invVolume of calcDerivFromFlux, per side
+    int skipDeriv[3];      // volume <= 1e-7: the side adds nothing
+    int zeroFlux[3];       // area <= 1e-7: calcFlux writes a zero flux
+    double gamma, rhoMin, PMin, cfl, fixed_dt, t_end;
+    long long max_steps;
+    void* buf[kMaxBufs];
+    void* dbuf[kMaxDBufs];
+};
+
+struct DevCtl {
+    double t, dt;
+    unsigned long long dtmin[2];   // FP64 bits of the CFL min (positive: order-preserving)
+    long long steps;
+    int active, stepping, done, status, par;
+    int rot;                       // 1: state buffers 0 and StageArgs::rot_buf are swapped for this slot
+};
+
+struct StageDev {
+    int in_buf, out_buf;
+    int n_alpha;
+    int alpha_buf[4];
+    double alpha[4];
+    int n_beta;
+    int beta_buf[4];
+    double beta[4];
+    double beta_cur;
+    int store_deriv;
+    int last;
+};
+
+struct StageArgs {
+    const DevInst* inst;
+    DevCtl* ctl;
+    const CUtensorMap* tmaps;   // [slot * kMaxBufs + buf]
+    const int4* items;          // {slot, tile x, tile y, tile z}
+    const int* nitems;
+    StageDev st;
+    int rot_buf;                // result buffer of a rotating plan (0: the plan does not rotate)
+    int* err;
+};
+
+// A slot whose step count left its state in the other buffer of a rotating
+// plan (forward Euler) sees buffers 0 and rot_buf exchanged.
+__device__ __forceinline__ int slotBuf(int b, int rot, int r) {
+    return rot ? (b == 0 ? r : (b == r ? 0 : b)) : b;
+}
+
+// ---------------------------------------------------------------------------
+// TMA / mbarrier
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: gives up after `limit` polls (each poll may itself suspend
+// for a short, hardware-chosen time).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned phase, unsigned limit) {
+    for (unsigned i = 0; i < limit; ++i)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+
+template <int RANK>
+__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, uint64_t* bar) {
+    uint64_t const m = reinterpret_cast<uint64_t>(map);
+    if (RANK == 2) {
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+            ::"r"(smem_u32(dst)), "l"(m), "r"(c0), "r"(c1), "r"(smem_u32(bar)) : "memory");
+    } else if (RANK == 3) {
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+            ::"r"(smem_u32(dst)), "l"(m), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar)) : "memory");
+    } else {
+        asm volatile(
+            "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+            ::"r"(smem_u32(dst)), "l"(m), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar)) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-cell helpers shared by the stage kernel and the auxiliary kernels
+// ---------------------------------------------------------------------------
+
+template <int DIM>
+__device__ __forceinline__ long long padIndex(const DevInst& I, int gx, int gy, int gz) {
+    long long const y = DIM > 1 ? gy + kG : 0;
+    long long const z = DIM > 2 ? gz + kG : 0;
+    return (z * I.py + y) * I.px + (gx + kG);
+}
+
+template <typename T>
+__device__ __forceinline__ ref::Eos refEos(const DevInst& I, int slopeLim, int fluxLim) {
+    ref::Eos e;
+    e.gamma = I.gamma; e.rhoMin = I.rhoMin; e.PMin = I.PMin;
+    e.fluxLimiter = fluxLim; e.slopeLimiter = slopeLim;
+    return e;
+}
+
+template <typename T>
+__device__ __forceinline__ fast::Eos<T> fastEos(const DevInst& I, int slopeLim, int fluxLim) {
+    fast::Eos<T> e;
+    e.gamma = T(I.gamma);
+    e.g1 = T(I.gamma - 1.);
+    e.rhoMin = T(I.rhoMin);
+    e.PMin = T(I.PMin);
+    e.fluxLimiter = fluxLim;
+    e.slopeLimiter = slopeLim;
+    return e;
+}
+
+// constrainU of one cell (global frame, 5 components).
+template <typename T, bool EXACT>
+__device__ __forceinline__ void constrainCell(T* u, const DevInst& I) {
+    if (EXACT) {
+        double U[6] = {(double)u[0], (double)u[1], (double)u[2], (double)u[3], (double)u[4], 0.};
+        ref::constrain(U, refEos<T>(I, 0, 0));
+        for (int j = 0; j < 5; ++j) u[j] = (T)U[j];
+    } else {
+        T const rhoMin = T(I.rhoMin), PMin = T(I.PMin), g1 = T(I.gamma - 1.);
+        if (u[0] < rhoMin) u[0] = rhoMin;
+        T const inv = fast::M<T>::rcp(u[0]);
+        T const vx = u[1] * inv, vy = u[2] * inv, vz = u[3] * inv;
+        T const m2 = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
+        T P = u[0] < rhoMin ? T(0) : g1 * (u[4] - T(.5) * m2 * inv);
+        if (P < PMin) P = PMin;
+        T const rho = u[0];
+        u[1] = vx * rho;
+        u[2] = vy * rho;
+        u[3] = vz * rho;
+        u[4] = rho * (T(.5) * (vx * vx + vy * vy + vz * vz)) + fast::M<T>::div(P, g1);
+    }
+}
+
+// calcDTCell of one cell (global frame).
+template <typename T, bool EXACT, int DIM>
+__device__ __forceinline__ double dtCell(const T* u, const DevInst& I) {
+    if (EXACT) {
+        double U[6] = {(double)u[0], (double)u[1], (double)u[2], (double)u[3], (double)u[4], 0.};
+        return ref::dtCell(U, refEos<T>(I, 0, 0), DIM, I.grid_dx);
+    } else {
+        T const rhoMin = T(I.rhoMin), PMin = T(I.PMin), g1 = T(I.gamma - 1.);
+        T const inv = fast::M<T>::rcp(u[0]);
+        T const m2 = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
+        T const P = u[0] < rhoMin ? T(0) : g1 * (u[4] - T(.5) * m2 * inv);
+        T const Cs = P <= PMin ? T(0) : (u[0] < rhoMin ? fast::M<T>::inf() : fast::M<T>::sqrt_(T(I.gamma) * P * inv));
+        T dt = fast::M<T>::inf();
+#pragma unroll
+        for (int side = 0; side < DIM; ++side) {
+            T const vn = u[0] < rhoMin ? T(0) : u[1 + side] * inv;
+            T a = fast::tmax(fabs(vn - Cs), fabs(vn + Cs));
+            a = fast::tmax(T(1e-9), a);
+            dt = fast::tmin(dt, fast::M<T>::div(T(I.grid_dx[side]), a));
+        }
+        return (double)dt;
+    }
+}
+
+// Writes a freshly computed interior cell into every ghost cell that the
+// boundary condition copies from it (gridsolver.lua:638-780): periodic wraps,
+// mirror reflects with the normal momentum negated, freeflow repeats the edge
+// cell.  Corner ghosts are never read by the dimension-split stencil and are
+// not written.
+template <typename T, int DIM>
+__device__ __forceinline__ void scatterGhosts(const DevInst& I, T* base, int gx, int gy, int gz, const T* u) {
+    int g[3] = {gx, gy, gz};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        int const c = g[d], N = I.n[d];
+        int tgt[4];
+        bool neg[4];
+        int nt = 0;
+        int const lo = I.bc[2 * d], hi = I.bc[2 * d + 1];
+        if (lo == HC_BOUNDARY_PERIODIC && c >= N - 2) { tgt[nt] = c - N; neg[nt++] = false; }
+        if (lo == HC_BOUNDARY_MIRROR && c <= 1) { tgt[nt] = -1 - c; neg[nt++] = true; }
+        if (lo == HC_BOUNDARY_FREEFLOW && c == 0) { tgt[nt] = -1; neg[nt++] = false; tgt[nt] = -2; neg[nt++] = false; }
+        if (hi == HC_BOUNDARY_PERIODIC && c <= 1) { tgt[nt] = N + c; neg[nt++] = false; }
+        if (hi == HC_BOUNDARY_MIRROR && c >= N - 2) { tgt[nt] = N + (N - 1 - c); neg[nt++] = true; }
+        if (hi == HC_BOUNDARY_FREEFLOW && c == N - 1) { tgt[nt] = N; neg[nt++] = false; tgt[nt] = N + 1; neg[nt++] = false; }
+        for (int k = 0; k < nt; ++k) {
+            int h[3] = {gx, gy, gz};
+            h[d] = tgt[k];
+            long long const idx = padIndex<DIM>(I, h[0], h[1], h[2]);
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                T v = u[f];
+                if (neg[k] && f == 1 + d) v = T(-1) * v;
+                base[f * I.plane + idx] = v;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// line sweeps
+// ---------------------------------------------------------------------------
+
+// Box geometry of a tile configuration.
+template <int DIM, int TX, int TY, int TZ>
+struct BoxGeom {
+    static constexpr int BX = TX + 4;
+    static constexpr int BY = DIM > 1 ? TY + 4 : 1;
+    static constexpr int BZ = DIM > 2 ? TZ + 4 : 1;
+    static constexpr int BOXN = BX * BY * BZ;
+    static constexpr int DPX = TX + 1;
+    static constexpr int DN = DIM > 1 ? DPX * TY * (DIM > 2 ? TZ : 1) : 0;
+    static constexpr int STRIDE[3] = {1, BX, BX * BY};
+};
+
+// Sweeps one segment of L cells along AXIS.  `base` is the box index of the
+// segment's first cell.  emit(k, FL, FR) receives, for cell k of the segment,
+// its left and right face fluxes in the global frame (5 components).
+template <typename T, int AXIS, int STRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, class Emit>
+__device__ __forceinline__ void sweepSegment(const T* box, int base, const DevInst& I, int slopeLim, int fluxLim,
+                                             double dt, Emit&& emit) {
+    if (EXACT) {
+        ref::Eos const e = refEos<T>(I, slopeLim, fluxLim);
+        double const dt_dx = dt / I.grid_dx[AXIS];
+        auto load = [&](int k, double* U) {
+#pragma unroll
+            for (int f = 0; f < 5; ++f) U[f] = (double)box[f * BOXN + base + k * STRIDE];
+            U[5] = 0.;
+        };
+        double Fprev[6], F[6];
+        bool const zero = I.zeroFlux[AXIS] != 0;
+        auto flux = [&](double* out, const double* UL, const double* UR, const ref::Iface& C,
+                        const ref::Iface* IL, const ref::Iface* IR) {
+            if (zero) { for (int j = 0; j < 6; ++j) out[j] = 0.; return; }
+            ref::roeFlux(out, e, UL, UR, C, IL, IR, AXIS, LIM, dt_dx);
+        };
+        if (PLM) {
+            double Um[6], U0[6], Up[6], prevR[6], fL[6], fR[6];
+            load(-2, Um);
+            load(-1, U0);
+            for (int k = -1; k <= L; ++k) {
+                load(k + 1, Up);
+                ref::plmCons(fL, fR, e, Um, U0, Up);
+                if (k >= 0) {
+                    ref::Iface C;
+                    ref::makeIface(C, e, prevR, fL, AXIS);
+                    flux(F, prevR, fL, C, &C, &C);
+                    if (k >= 1) emit(k - 1, Fprev, F);
+                    for (int j = 0; j < 6; ++j) Fprev[j] = F[j];
+                }
+                for (int j = 0; j < 6; ++j) { prevR[j] = fR[j]; Um[j] = U0[j]; U0[j] = Up[j]; }
+            }
+        } else if (LIM) {
+            double Ua[6], Ub[6], Uc[6], Ud[6];
+            ref::Iface IL, IC, IR;
+            load(-2, Ua);
+            load(-1, Ub);
+            load(0, Uc);
+            ref::makeIface(IL, e, Ua, Ub, AXIS);
+            ref::makeIface(IC, e, Ub, Uc, AXIS);
+            for (int k = 0; k <= L; ++k) {
+                load(k + 1, Ud);
+                ref::makeIface(IR, e, Uc, Ud, AXIS);
+                flux(F, Ub, Uc, IC, &IL, &IR);
+                if (k >= 1) emit(k - 1, Fprev, F);
+                for (int j = 0; j < 6; ++j) { Fprev[j] = F[j]; Ub[j] = Uc[j]; Uc[j] = Ud[j]; }
+                IL = IC;
+                IC = IR;
+            }
+        } else {
+            double Ua[6], Ub[6];
+            load(-1, Ua);
+            for (int k = 0; k <= L; ++k) {
+                load(k, Ub);
+                ref::Iface C;
+                ref::makeIface(C, e, Ua, Ub, AXIS);
+                flux(F, Ua, Ub, C, &C, &C);
+                if (k >= 1) emit(k - 1, Fprev, F);
+                for (int j = 0; j < 6; ++j) { Fprev[j] = F[j]; Ua[j] = Ub[j]; }
+            }
+        }
+    } else {
+        using C5 = fast::C5<T>;
+        fast::Eos<T> const e = fastEos<T>(I, slopeLim, fluxLim);
+        T const dt_dx = T(dt / I.grid_dx[AXIS]);
+        constexpr int A1 = 1 + AXIS, A2 = 1 + (AXIS + 1) % 3, A3 = 1 + (AXIS + 2) % 3;
+        // loads in the interface frame (rho, m_n, m_t1, m_t2, E)
+        auto load = [&](int k, C5& U) {
+            int const i = base + k * STRIDE;
+            U.u[0] = box[0 * BOXN + i];
+            U.u[1] = box[A1 * BOXN + i];
+            U.u[2] = box[A2 * BOXN + i];
+            U.u[3] = box[A3 * BOXN + i];
+            U.u[4] = box[4 * BOXN + i];
+        };
+        bool const zero = I.zeroFlux[AXIS] != 0;
+        // flux in the interface frame, then back to the global frame
+        T Fprev[5], F[5];
+        auto flux = [&](T* out, const C5& UL, const C5& UR, const fast::IfaceF<T>& C,
+                        const fast::IfaceF<T>& IL, const fast::IfaceF<T>& IR) {
+            T Fr[5];
+            fast::roe<T, LIM>(Fr, e, UL, UR, C, IL, IR, dt_dx);
+            if (zero) for (int j = 0; j < 5; ++j) Fr[j] = T(0);
+            out[0] = Fr[0];
+            out[A1] = Fr[1];
+            out[A2] = Fr[2];
+            out[A3] = Fr[3];
+            out[4] = Fr[4];
+        };
+        if (PLM) {
+            C5 Um, U0, Up, prevR, fL, fR;
+            load(-2, Um);
+            load(-1, U0);
+#pragma unroll 1
+            for (int k = -1; k <= L; ++k) {
+                load(k + 1, Up);
+#pragma unroll
+                for (int j = 0; j < 5; ++j) {
+                    T const sg = T(.5) * fast::plmSigma<T>(Um.u[j], U0.u[j], Up.u[j], slopeLim);
+                    fL.u[j] = U0.u[j] - sg;
+                    fR.u[j] = U0.u[j] + sg;
+                }
+                if (k >= 0) {
+                    fast::IfaceF<T> C;
+                    fast::makeIface(C, e, prevR, fL);
+                    flux(F, prevR, fL, C, C, C);
+                    if (k >= 1) emit(k - 1, Fprev, F);
+#pragma unroll
+                    for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
+                }
+                prevR = fR;
+                Um = U0;
+                U0 = Up;
+            }
+        } else if (LIM) {
+            C5 Ua, Ub, Uc, Ud;
+            fast::IfaceF<T> IL, IC, IR;
+            load(-2, Ua);
+            load(-1, Ub);
+            load(0, Uc);
+            fast::makeIface(IL, e, Ua, Ub);
+            fast::makeIface(IC, e, Ub, Uc);
+#pragma unroll 1
+            for (int k = 0; k <= L; ++k) {
+                load(k + 1, Ud);
+                fast::makeIface(IR, e, Uc, Ud);
+                flux(F, Ub, Uc, IC, IL, IR);
+                if (k >= 1) emit(k - 1, Fprev, F);
+#pragma unroll
+                for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
+                Ub = Uc;
+                Uc = Ud;
+                IL = IC;
+                IC = IR;
+            }
+        } else {
+            C5 Ua, Ub;
+            load(-1, Ua);
+#pragma unroll 1
+            for (int k = 0; k <= L; ++k) {
+                load(k, Ub);
+                fast::IfaceF<T> C;
+                fast::makeIface(C, e, Ua, Ub);
+                flux(F, Ua, Ub, C, C, C);
+                if (k >= 1) emit(k - 1, Fprev, F);
+#pragma unroll
+                for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
+                Ua = Ub;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the stage kernel
+// ---------------------------------------------------------------------------
+
+template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT>
+struct StageCfg {
+    using G = BoxGeom<DIM, TX, TY, TZ>;
+    static constexpr size_t kBarOff = (((size_t)(5 * G::BOXN + 5 * G::DN) * sizeof(T)) + 15) / 16 * 16;
+    static constexpr size_t SMEM = kBarOff + 16;
+    static constexpr unsigned BYTES = (unsigned)(5 * G::BOXN * sizeof(T));
+    static_assert(G::BX <= 256 && G::BY <= 256 && G::BZ <= 256, "TMA box extent");
+    static_assert((G::BX * sizeof(T)) % 16 == 0, "TMA box rows must be a multiple of 16 bytes");
+    static_assert(TX % L == 0 && (DIM < 2 || TY % L == 0) && (DIM < 3 || TZ % L == 0), "segments tile the box");
+};
+
+constexpr unsigned kSpinLimit = 1u << 22;
+
+template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM>
+__global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs a, int slopeLim, int fluxLim) {
+    using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
+    using G = typename Cfg::G;
+    extern __shared__ __align__(128) unsigned char smem[];
+    T* box = reinterpret_cast<T*>(smem);
+    T* D = box + 5 * G::BOXN;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Cfg::kBarOff);
+    int const tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    int const nitems = *a.nitems;
+    unsigned phase = 0;
+    const StageDev& st = a.st;
+
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        int4 const it = a.items[item];
+        const DevInst& I = a.inst[it.x];
+        DevCtl* ctl = a.ctl + it.x;
+        if (!ctl->stepping) continue;
+        int const x0 = it.y * TX, y0 = it.z * TY, z0 = it.w * TZ;
+        int const rot = ctl->rot;
+        int const inBuf = slotBuf(st.in_buf, rot, a.rot_buf);
+
+        if (tid == 0) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(bar, Cfg::BYTES);
+            const CUtensorMap* map = a.tmaps + (size_t)it.x * kMaxBufs + inBuf;
+            if (DIM == 1) tma_load<2>(box, map, x0, 0, 0, 0, bar);
+            else if (DIM == 2) tma_load<3>(box, map, x0, y0, 0, 0, bar);
+            else tma_load<4>(box, map, x0, y0, z0, 0, bar);
+        }
+        if (!mbar_wait_bounded(bar, phase, kSpinLimit)) {
+            // the copy did not complete: record it, give the copy a second
+            // bounded chance to land before the CTA releases its smem, stop
+            if (tid == 0) { atomicOr(a.err, DEV_TIMEOUT); atomicOr(&ctl->status, DEV_TIMEOUT); }
+            mbar_wait_bounded(bar, phase, kSpinLimit);
+            return;
+        }
+        phase ^= 1u;
+
+        double const dt = ctl->dt;
+        int const nx = I.n[0], ny = I.n[1], nz = I.n[2];
+
+        // ---- all axes but the last: flux differences into D ----------------
+        if (DIM >= 2) {
+#pragma unroll 1
+            for (int axis = 0; axis < DIM - 1; ++axis) {
+                if (axis == 0) {
+                    constexpr int nlines = TY * (DIM > 2 ? TZ : 1);
+                    constexpr int nseg = TX / L;
+                    double const ar = I.area[0];
+                    bool const skip = I.skipDeriv[0] != 0;
+                    for (int t = tid; t < nlines * nseg; t += NT) {
+                        int const line = t % nlines, seg = t / nlines;
+                        int const cy = line % TY, cz = line / TY;
+                        int const cx0 = seg * L;
+                        if (x0 + cx0 >= nx || y0 + cy >= ny || z0 + cz >= nz) continue;
+                        int const base = ((cz + (DIM > 2 ? 2 : 0)) * G::BY + (cy + 2)) * G::BX + (cx0 + 2);
+                        T* Dl = D + (cz * TY + cy) * G::DPX + cx0;
+                        sweepSegment<T, 0, 1, G::BOXN, L, EXACT, PLM, LIM>(box, base, I, slopeLim, fluxLim, dt,
+                            [&](int k, const auto* FL, const auto* FR) {
+#pragma unroll
+                                for (int f = 0; f < 5; ++f) {
+                                    T d = T(0);
+                                    if (!skip) d = T(0) - (T(FR[f]) * T(ar) - T(FL[f]) * T(ar));
+                                    Dl[f * G::DN + k] = d;
+                                }
+                            });
+                    }
+                } else {
+                    // axis 1 of a 3D tile (only reached when DIM == 3)
+                    constexpr int nlines = TX * TZ;
+                    constexpr int nseg = TY / L;
+                    double const ar = I.area[1];
+                    bool const skip = I.skipDeriv[1] != 0;
+                    for (int t = tid; t < nlines * nseg; t += NT) {
+                        int const cx = t % TX, rest = t / TX;
+                        int const cz = rest % TZ, seg = rest / TZ;
+                        int const cy0 = seg * L;
+                        if (x0 + cx >= nx || y0 + cy0 >= ny || z0 + cz >= nz) continue;
+                        int const base = ((cz + 2) * G::BY + (cy0 + 2)) * G::BX + (cx + 2);
+                        T* Dl = D + (cz * TY + cy0) * G::DPX + cx;
+                        sweepSegment<T, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM>(box, base, I, slopeLim, fluxLim, dt,
+                            [&](int k, const auto* FL, const auto* FR) {
+#pragma unroll
+                                for (int f = 0; f < 5; ++f) {
+                                    T& d = Dl[f * G::DN + k * G::DPX];
+                                    if (!skip) d = d - (T(FR[f]) * T(ar) - T(FL[f]) * T(ar));
+                                }
+                            });
+                    }
+                }
+                __syncthreads();
+            }
+        }
+
+        // ---- last axis: finish each cell ------------------------------------
+        constexpr int AX = DIM - 1;
+        constexpr int TA = AX == 0 ? TX : (AX == 1 ? TY : TZ);
+        constexpr int nlines = (TX * TY * TZ) / TA / (DIM < 2 ? TY : 1) / (DIM < 3 ? TZ : 1);
+        constexpr int nseg = TA / L;
+        constexpr int STRIDE_AX = AX == 0 ? 1 : (AX == 1 ? G::BX : G::BX * G::BY);
+
+        // stage coefficients (the reference casts beta * dt to real)
+        T calpha[4], cbeta[4];
+        for (int k = 0; k < 4; ++k) {
+            calpha[k] = k < st.n_alpha ? T(st.alpha[k]) : T(0);
+            cbeta[k] = k < st.n_beta ? T(st.beta[k] * dt) : T(0);
+        }
+        T const cbcur = T(st.beta_cur * dt);
+        T* out = reinterpret_cast<T*>(I.buf[slotBuf(st.out_buf, rot, a.rot_buf)]);
+        T* dstore = st.store_deriv >= 0 ? reinterpret_cast<T*>(I.dbuf[st.store_deriv]) : nullptr;
+        double const ar = I.area[AX];
+        bool const skip = I.skipDeriv[AX] != 0;
+        double dtmin = __longlong_as_double((long long)kInfBits);
+        bool bad = false;
+
+        for (int t = tid; t < nlines * nseg; t += NT) {
+            int cx, cy, cz, seg;
+            if (DIM == 1) { cx = 0; cy = 0; cz = 0; seg = t; }
+            else if (DIM == 2) { cx = t % TX; seg = t / TX; cy = 0; cz = 0; }
+            else { cx = t % TX; cy = (t / TX) % TY; seg = t / (TX * TY); cz = 0; }
+            int c0[3] = {cx, cy, cz};
+            c0[AX] = seg * L;
+            int const gx0 = x0 + c0[0], gy0 = y0 + c0[1], gz0 = z0 + c0[2];
+            if (gx0 >= nx || gy0 >= ny || gz0 >= nz) continue;
+            int const base = ((c0[2] + (DIM > 2 ? 2 : 0)) * G::BY + (c0[1] + (DIM > 1 ? 2 : 0))) * G::BX + (c0[0] + 2);
+            int const dbase = (c0[2] * TY + c0[1]) * G::DPX + c0[0];
+            sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM>(box, base, I, slopeLim, fluxLim, dt,
+                [&](int k, const auto* FL, const auto* FR) {
+                    int g[3] = {gx0, gy0, gz0};
+                    g[AX] += k;
+                    if (g[AX] >= I.n[AX]) return;
+                    T u[5], deriv[5];
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) {
+                        T d = DIM > 1 ? D[f * G::DN + dbase + k * (AX == 1 ? G::DPX : (AX == 2 ? G::DPX * TY : 1))] : T(0);
+                        if (!skip) d = d - (T(FR[f]) * T(ar) - T(FL[f]) * T(ar));
+                        deriv[f] = d;
+                    }
+                    long long const idx = padIndex<DIM>(I, g[0], g[1], g[2]);
+                    // u = sum alpha_k u^(k) + sum (beta_k dt) L(u^(k)) + (beta_cur dt) deriv
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) u[f] = T(0);
+                    for (int m = 0; m < st.n_alpha; ++m) {
+                        int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
+                        if (b == inBuf) {
+#pragma unroll
+                            for (int f = 0; f < 5; ++f) u[f] = u[f] + box[f * G::BOXN + base + k * STRIDE_AX] * calpha[m];
+                        } else {
+                            const T* src = reinterpret_cast<const T*>(I.buf[b]);
+#pragma unroll
+                            for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * calpha[m];
+                        }
+                    }
+                    for (int m = 0; m < st.n_beta; ++m) {
+                        const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * cbeta[m];
+                    }
+                    if (st.beta_cur != 0.) {
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) u[f] = u[f] + deriv[f] * cbcur;
+                    }
+                    constrainCell<T, EXACT>(u, I);
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) {
+                        out[f * I.plane + idx] = u[f];
+                        bad |= !isfinite((double)u[f]);
+                    }
+                    scatterGhosts<T, DIM>(I, out, g[0], g[1], g[2], u);
+                    if (dstore) {
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) dstore[f * I.plane + idx] = deriv[f];
+                    }
+                    if (st.last) dtmin = fmin(dtmin, dtCell<T, EXACT, DIM>(u, I));
+                });
+        }
+
+        // one FP64 atomicMin per warp for the next step's CFL dt
+        if (st.last) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) dtmin = fmin(dtmin, __shfl_xor_sync(0xffffffffu, dtmin, o));
+            if ((tid & 31) == 0 && dtmin < __longlong_as_double((long long)kInfBits))
+                atomicMin(&ctl->dtmin[ctl->par ^ 1], (unsigned long long)__double_as_longlong(dtmin));
+        }
+        if (__any_sync(0xffffffffu, bad) && (tid & 31) == 0) atomicOr(&ctl->status, DEV_NONFINITE);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// auxiliary kernels (per slot)
+// ---------------------------------------------------------------------------
+
+// Finishes a pending step (t += dt) and begins the next one for every slot:
+// the App's exit test (t >= t_end, before stepping), then dt = cfl * min.
+__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates);
+
+template <typename T, int DIM>
+__global__ void k_fill_ghosts(const DevInst* inst, int slot, int buf) {
+    const DevInst& I = inst[slot];
+    T* base = reinterpret_cast<T*>(I.buf[buf]);
+    long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
+        bool edge = false;
+        int g[3] = {gx, gy, gz};
+        for (int d = 0; d < DIM; ++d) edge |= g[d] < 2 || g[d] >= I.n[d] - 2;
+        if (!edge) continue;
+        long long const idx = padIndex<DIM>(I, gx, gy, gz);
+        T u[5];
+        for (int f = 0; f < 5; ++f) u[f] = base[f * I.plane + idx];
+        scatterGhosts<T, DIM>(I, base, gx, gy, gz, u);
+    }
+}
+
+template <typename T, int DIM, bool EXACT>
+__global__ void k_constrain(const DevInst* inst, int slot, int buf) {
+    const DevInst& I = inst[slot];
+    T* base = reinterpret_cast<T*>(I.buf[buf]);
+    long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
+        long long const idx = padIndex<DIM>(I, gx, gy, gz);
+        T u[5];
+        for (int f = 0; f < 5; ++f) u[f] = base[f * I.plane + idx];
+        constrainCell<T, EXACT>(u, I);
+        for (int f = 0; f < 5; ++f) base[f * I.plane + idx] = u[f];
+    }
+}
+
+// calcDT of one slot's current state into ctl.dtmin[ctl.par] (reset first by the host).
+template <typename T, int DIM, bool EXACT>
+__global__ void k_calc_dt(const DevInst* inst, DevCtl* ctl, int slot, int buf) {
+    const DevInst& I = inst[slot];
+    const T* base = reinterpret_cast<const T*>(I.buf[buf]);
+    long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
+    double m = __longlong_as_double((long long)kInfBits);
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
+        long long const idx = padIndex<DIM>(I, gx, gy, gz);
+        T u[5];
+        for (int f = 0; f < 5; ++f) u[f] = base[f * I.plane + idx];
+        m = fmin(m, dtCell<T, EXACT, DIM>(u, I));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m < __longlong_as_double((long long)kInfBits))
+        atomicMin(&ctl[slot].dtmin[ctl[slot].par], (unsigned long long)__double_as_longlong(m));
+}
+
+// Interior <-> staging transfer with layout conversion (dir 0: staging -> grid).
+template <typename T, int DIM>
+__global__ void k_xfer(const DevInst* inst, int slot, int buf, void* staging, int layout, int dir) {
+    const DevInst& I = inst[slot];
+    T* base = reinterpret_cast<T*>(I.buf[buf]);
+    long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
+        long long const idx = padIndex<DIM>(I, gx, gy, gz);
+        for (int f = 0; f < 5; ++f) {
+            T* g = base + f * I.plane + idx;
+            if (layout == HC_LAYOUT_AOS6_F64) {
+                double* h = (double*)staging + 6 * k + f;
+                if (dir == 0) *g = (T)*h; else *h = (double)*g;
+            } else if (layout == HC_LAYOUT_SOA5_F64) {
+                double* h = (double*)staging + f * n + k;
+                if (dir == 0) *g = (T)*h; else *h = (double)*g;
+            } else {
+                float* h = (float*)staging + f * n + k;
+                if (dir == 0) *g = (T)*h; else *h = (float)*g;
+            }
+        }
+        if (layout == HC_LAYOUT_AOS6_F64 && dir == 1) ((double*)staging)[6 * k + 5] = 0.;
+    }
+}
+
+// Kahan-compensated FP64 sums of the 5 fields times the cell volume; one
+// partial per block, combined on the host in block order.
+template <typename T, int DIM>
+__global__ void k_sums(const DevInst* inst, int slot, int buf, double vol, double* partial) {
+    const DevInst& I = inst[slot];
+    const T* base = reinterpret_cast<const T*>(I.buf[buf]);
+    long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
+    double s[5] = {0, 0, 0, 0, 0}, c[5] = {0, 0, 0, 0, 0};
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
+        long long const idx = padIndex<DIM>(I, gx, gy, gz);
+        for (int f = 0; f < 5; ++f) {
+            double const y = (double)base[f * I.plane + idx] * vol - c[f];
+            double const tt = s[f] + y;
+            c[f] = (tt - s[f]) - y;
+            s[f] = tt;
+        }
+    }
+    __shared__ double sh[5][256];
+    for (int f = 0; f < 5; ++f) sh[f][threadIdx.x] = s[f];
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        int const f = threadIdx.x;
+        double sm = 0, cc = 0;
+        for (int k = 0; k < (int)blockDim.x; ++k) {
+            double const y = sh[f][k] - cc;
+            double const tt = sm + y;
+            cc = (tt - sm) - y;
+            sm = tt;
+        }
+        partial[5 * blockIdx.x + f] = sm;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launcher registry
+// ---------------------------------------------------------------------------
+
+struct StageLauncher {
+    int precision;   // HC_F32_FUSED / HC_F64_FUSED
+    int dim;
+    bool plm, lim;
+    int variant;     // tile-shape candidate index
+    int tx, ty, tz, nthreads;
+    size_t smem;
+    void (*launch)(const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s);
+    int (*occupancy)();   // CTAs per SM (sets the smem attribute first); <= 0 on error
+};
+
+struct AuxLauncher {
+    int precision;
+    int dim;
+    void (*fill_ghosts)(const DevInst* inst, int slot, int buf, cudaStream_t s);
+    void (*constrain)(const DevInst* inst, int slot, int buf, cudaStream_t s);
+    void (*calc_dt)(const DevInst* inst, DevCtl* ctl, int slot, int buf, cudaStream_t s);
+    void (*xfer)(const DevInst* inst, int slot, int buf, void* staging, int layout, int dir, cudaStream_t s);
+    void (*sums)(const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s);
+};
+
+void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& aux);
+
+}  // namespace fz
+}  // namespace hc

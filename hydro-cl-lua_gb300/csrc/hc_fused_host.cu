@@ -1,0 +1,826 @@
+// hc_fused_host.cu -- host side of the fused form: a set of instances
+// (slots) that advance together, each with its own grid, boundary, CFL dt and
+// end time, sharing one scheme (reconstruction, limiters, integrator).
+//
+// Per step: k_begin (per-slot exit test and CFL dt, on the device), then one
+// persistent launch of the stage kernel per Runge-Kutta stage and per grid
+// dimension present, each walking a work list of (slot, tile) items.  The
+// step is captured once into a CUDA graph and replayed; the work lists and
+// the per-slot control blocks live in device memory, so the graph stays valid
+// while instances come and go (it is re-captured only when a work-list
+// buffer is reallocated or the set of dimensions changes).
+#include "hc_internal.h"
+#include "hc_fused.cuh"
+
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+
+namespace hc {
+
+using namespace fz;
+
+namespace fz {
+
+__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates) {
+    int const s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    DevCtl& c = ctl[s];
+    if (c.stepping) {
+        c.t = c.t + c.dt;       // solverbase.lua:3168
+        c.steps += 1;
+        c.stepping = 0;
+        c.par ^= 1;
+        c.rot ^= rotates;
+    }
+    if (!begin) return;
+    c.dtmin[c.par ^ 1] = kInfBits;
+    if (!c.active) return;
+    const DevInst& I = inst[s];
+    if (c.status != 0) { c.active = 0; c.done = 1; return; }
+    // app.lua:1590: the exit test precedes the update
+    if (c.t >= I.t_end || c.steps >= I.max_steps) { c.active = 0; c.done = 1; return; }
+    double const dt = I.fixed_dt > 0 ? I.fixed_dt : I.cfl * __longlong_as_double((long long)c.dtmin[c.par]);
+    if (!(dt > 0) || !isfinite(dt)) { c.status = DEV_NONFINITE; c.active = 0; c.done = 1; return; }
+    c.dt = dt;
+    c.stepping = 1;
+}
+
+// Explicit-dt step of one slot (SolverBase:step(dt): t is not advanced).
+__global__ void k_set_dt(DevCtl* ctl, int slot, double dt, int on, int rotates) {
+    DevCtl& c = ctl[slot];
+    if (on) {
+        c.dtmin[c.par ^ 1] = kInfBits;
+        c.dt = dt;
+        c.stepping = 1;
+    } else {
+        c.stepping = 0;
+        c.par ^= 1;
+        c.rot ^= rotates;
+    }
+}
+
+// For timing a stage in isolation: mark live slots as stepping with their
+// current CFL dt, without touching t, steps or the dt parity.
+__global__ void k_tune_mode(DevCtl* ctl, const DevInst* inst, int nslots, int on) {
+    int const s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    DevCtl& c = ctl[s];
+    if (!on) { c.stepping = 0; return; }
+    if (!c.active) return;
+    const DevInst& I = inst[s];
+    double const dt = I.fixed_dt > 0 ? I.fixed_dt : I.cfl * __longlong_as_double((long long)c.dtmin[c.par]);
+    c.dt = isfinite(dt) && dt > 0 ? dt : 0.;
+    c.stepping = 1;
+}
+
+__global__ void k_reset_dtmin(DevCtl* ctl, int slot) {
+    ctl[slot].dtmin[ctl[slot].par] = kInfBits;
+}
+
+}  // namespace fz
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int get_encoder() {
+    if (g_encode) return HC_OK;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return fail(HC_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    return HC_OK;
+}
+
+struct Registry {
+    std::vector<StageLauncher> st;
+    std::vector<AuxLauncher> aux;
+    Registry() { register_launchers(st, aux); }
+};
+const Registry& registry() {
+    static Registry r;
+    return r;
+}
+const std::vector<StageLauncher>& stage_launchers() { return registry().st; }
+const std::vector<AuxLauncher>& aux_launchers() { return registry().aux; }
+
+size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct Slot {
+    bool used = false;
+    hc_solver_desc d;
+    int dim = 0;
+    size_t bytes = 0;
+    void* mem = nullptr;
+    DevInst inst;
+    long long cells = 0;
+};
+
+struct FusedSet {
+    FusedScheme sch;
+    IntegratorPlan plan[1];        // stages from state buffer 0
+    bool rotates = false;          // the plan leaves the state in plan.result_buf (per-slot DevCtl::rot)
+    int rot_buf = 0;
+    int esize = 4;
+    int max_slots = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    std::vector<Slot> slots;
+    DevInst* d_inst = nullptr;
+    DevCtl* d_ctl = nullptr;
+    CUtensorMap* d_tmaps = nullptr;
+    std::vector<CUtensorMap> h_tmaps;
+    int* d_err = nullptr;
+    DevCtl* h_ctl = nullptr;       // pinned mirror
+    double* d_partial = nullptr;
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+    // work lists per dimension
+    int4* d_items[3] = {nullptr, nullptr, nullptr};
+    size_t items_cap[3] = {0, 0, 0};
+    int* d_nitems = nullptr;       // [3]
+    int h_nitems[3] = {0, 0, 0};
+    bool items_dirty = true;
+    // chosen tile-shape variant per dimension
+    const StageLauncher* launcher[3] = {nullptr, nullptr, nullptr};
+    int grid[3] = {0, 0, 0};
+    // graph of one (or two, when the state rotates) steps
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    int graph_dims_mask = 0;
+};
+
+static const StageLauncher* find_launcher(const FusedScheme& sch, int dim, int variant) {
+    bool const plm = sch.recon == HC_RECON_PLM_CONS;
+    bool const lim = sch.flux_limiter > 0;
+    for (const StageLauncher& L : stage_launchers())
+        if (L.precision == sch.precision && L.dim == dim && L.plm == plm && L.lim == lim && L.variant == variant) return &L;
+    return nullptr;
+}
+
+static const AuxLauncher* find_aux(int precision, int dim) {
+    for (const AuxLauncher& A : aux_launchers())
+        if (A.precision == precision && A.dim == dim) return &A;
+    return nullptr;
+}
+
+static int set_launcher(FusedSet* f, int dim, int variant) {
+    const StageLauncher* L = find_launcher(f->sch, dim, variant);
+    if (!L) return fail(HC_ERR_INVALID, "no stage kernel for this scheme / dimension / variant");
+    int const occ = L->occupancy();
+    if (occ <= 0) return fail(HC_ERR_CUDA, "stage kernel cannot be resident (shared memory / registers)");
+    f->launcher[dim - 1] = L;
+    f->grid[dim - 1] = f->num_sms * occ;
+    return HC_OK;
+}
+
+int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, FusedSet** out) {
+    if (sch.precision != HC_F32_FUSED && sch.precision != HC_F64_FUSED) return fail(HC_ERR_INVALID, "fused precision");
+    if (sch.recon != HC_RECON_NONE && sch.flux_limiter > 0)
+        return fail(HC_ERR_INVALID, "usePLM together with a flux limiter (gridsolver.lua:119 asserts against it)");
+    if (sch.integrator < 0 || sch.integrator >= HC_NUM_INTEGRATORS) return fail(HC_ERR_INVALID, "integrator");
+    if (sch.flux_limiter < 0 || sch.flux_limiter >= HC_NUM_LIMITERS || sch.slope_limiter < 0 || sch.slope_limiter >= HC_NUM_LIMITERS)
+        return fail(HC_ERR_INVALID, "limiter");
+    if (max_slots <= 0) return fail(HC_ERR_INVALID, "max_slots");
+    HC_CHECK(get_encoder());
+    FusedSet* f = new FusedSet();
+    f->sch = sch;
+    f->esize = sch.precision == HC_F32_FUSED ? 4 : 8;
+    f->max_slots = max_slots;
+    f->stream = stream;
+    f->plan[0] = make_plan(sch.integrator);
+    f->rotates = f->plan[0].result_buf != 0;
+    f->rot_buf = f->rotates ? f->plan[0].result_buf : 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&f->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    f->slots.resize(max_slots);
+    f->h_tmaps.resize((size_t)max_slots * kMaxBufs);
+    std::memset(f->h_tmaps.data(), 0, f->h_tmaps.size() * sizeof(CUtensorMap));
+    int r = HC_OK;
+    auto A = [&](void** p, size_t b) {
+        if (r != HC_OK) return;
+        cudaError_t e = cudaMalloc(p, b);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMalloc");
+    };
+    A((void**)&f->d_inst, sizeof(DevInst) * max_slots);
+    A((void**)&f->d_ctl, sizeof(DevCtl) * max_slots);
+    A((void**)&f->d_tmaps, sizeof(CUtensorMap) * kMaxBufs * max_slots);
+    A((void**)&f->d_err, sizeof(int));
+    A((void**)&f->d_nitems, sizeof(int) * 3);
+    A((void**)&f->d_partial, sizeof(double) * 5 * 1024);
+    if (r == HC_OK) {
+        cudaError_t e = cudaMallocHost((void**)&f->h_ctl, sizeof(DevCtl) * max_slots);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMallocHost");
+    }
+    if (r == HC_OK) {
+        cudaMemsetAsync(f->d_inst, 0, sizeof(DevInst) * max_slots, stream);
+        cudaMemsetAsync(f->d_ctl, 0, sizeof(DevCtl) * max_slots, stream);
+        cudaMemsetAsync(f->d_tmaps, 0, sizeof(CUtensorMap) * kMaxBufs * max_slots, stream);
+        cudaMemsetAsync(f->d_err, 0, sizeof(int), stream);
+        cudaMemsetAsync(f->d_nitems, 0, sizeof(int) * 3, stream);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMemsetAsync");
+    }
+    for (int dim = 1; dim <= 3 && r == HC_OK; ++dim) r = set_launcher(f, dim, 0);
+    if (r != HC_OK) {
+        fused_destroy(f);
+        return r;
+    }
+    *out = f;
+    return HC_OK;
+}
+
+void fused_destroy(FusedSet* f) {
+    if (!f) return;
+    if (f->stream) cudaStreamSynchronize(f->stream);
+    for (Slot& s : f->slots) if (s.mem) cudaFree(s.mem);
+    cudaFree(f->d_inst);
+    cudaFree(f->d_ctl);
+    cudaFree(f->d_tmaps);
+    cudaFree(f->d_err);
+    cudaFree(f->d_nitems);
+    cudaFree(f->d_partial);
+    cudaFree(f->staging);
+    for (int d = 0; d < 3; ++d) cudaFree(f->d_items[d]);
+    if (f->h_ctl) cudaFreeHost(f->h_ctl);
+    if (f->graph) cudaGraphExecDestroy(f->graph);
+    delete f;
+}
+
+static void padded_dims(const hc_solver_desc& d, int& px, int& py, int& pz) {
+    px = (int)round_up((size_t)d.n[0] + 2 * kG, 32);
+    py = d.dim > 1 ? d.n[1] + 2 * kG : 1;
+    pz = d.dim > 2 ? d.n[2] + 2 * kG : 1;
+}
+
+size_t fused_instance_bytes(const FusedSet* f, const hc_solver_desc& d) {
+    int px, py, pz;
+    padded_dims(d, px, py, pz);
+    size_t const planeBytes = round_up((size_t)px * py * pz * f->esize, 256);
+    return planeBytes * 5 * (size_t)(f->plan[0].n_state_bufs + f->plan[0].n_deriv_bufs);
+}
+
+static int validate(const FusedSet* f, const hc_solver_desc& d) {
+    if (d.dim < 1 || d.dim > 3) return fail(HC_ERR_INVALID, "dim must be 1, 2 or 3");
+    for (int k = 0; k < d.dim; ++k) {
+        if (d.n[k] < 2) return fail(HC_ERR_INVALID, "each active axis needs at least 2 cells");
+        if (d.n[k] > (1 << 24)) return fail(HC_ERR_INVALID, "grid axis too large");
+        if (!(d.maxs[k] > d.mins[k])) return fail(HC_ERR_INVALID, "maxs must exceed mins");
+    }
+    for (int k = 0; k < 2 * d.dim; ++k)
+        if (d.boundary[k] != HC_BOUNDARY_PERIODIC && d.boundary[k] != HC_BOUNDARY_MIRROR && d.boundary[k] != HC_BOUNDARY_FREEFLOW)
+            return fail(HC_ERR_INVALID, "the fused form supports periodic, mirror and freeflow boundaries");
+    for (int k = 0; k < d.dim; ++k)
+        if ((d.boundary[2 * k] == HC_BOUNDARY_PERIODIC) != (d.boundary[2 * k + 1] == HC_BOUNDARY_PERIODIC))
+            return fail(HC_ERR_INVALID, "periodic boundaries must be periodic on both sides of an axis");
+    if (!(d.gamma > 1.)) return fail(HC_ERR_INVALID, "gamma must exceed 1");
+    (void)f;
+    return HC_OK;
+}
+
+// Tensor maps of a slot's state buffers for the launcher's box.
+static int encode_maps(FusedSet* f, int slot) {
+    Slot& S = f->slots[slot];
+    const StageLauncher* L = f->launcher[S.dim - 1];
+    const DevInst& I = S.inst;
+    CUtensorMapDataType const dt = f->esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    int const rank = S.dim + 1;
+    cuuint64_t gdim[5], gstride[4];
+    cuuint32_t box[5], estride[5] = {1, 1, 1, 1, 1};
+    size_t const es = f->esize;
+    gdim[0] = I.px;
+    box[0] = L->tx + 4;
+    if (S.dim == 1) {
+        gdim[1] = 5; box[1] = 5;
+        gstride[0] = I.plane * es;
+    } else if (S.dim == 2) {
+        gdim[1] = I.py; gdim[2] = 5;
+        box[1] = L->ty + 4; box[2] = 5;
+        gstride[0] = (cuuint64_t)I.px * es;
+        gstride[1] = I.plane * es;
+    } else {
+        gdim[1] = I.py; gdim[2] = I.pz; gdim[3] = 5;
+        box[1] = L->ty + 4; box[2] = L->tz + 4; box[3] = 5;
+        gstride[0] = (cuuint64_t)I.px * es;
+        gstride[1] = (cuuint64_t)I.px * I.py * es;
+        gstride[2] = I.plane * es;
+    }
+    for (int b = 0; b < f->plan[0].n_state_bufs; ++b) {
+        CUtensorMap* m = &f->h_tmaps[(size_t)slot * kMaxBufs + b];
+        CUresult r = g_encode(m, dt, rank, I.buf[b], gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(HC_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    }
+    HC_CUDA(cudaMemcpyAsync(f->d_tmaps + (size_t)slot * kMaxBufs, &f->h_tmaps[(size_t)slot * kMaxBufs],
+                            sizeof(CUtensorMap) * kMaxBufs, cudaMemcpyHostToDevice, f->stream));
+    return HC_OK;
+}
+
+static int ensure_staging(FusedSet* f, size_t bytes) {
+    if (f->staging_bytes >= bytes) return HC_OK;
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    cudaFree(f->staging);
+    f->staging = nullptr;
+    f->staging_bytes = 0;
+    size_t const cap = std::max(bytes, (size_t)1 << 20);
+    HC_CUDA(cudaMalloc(&f->staging, cap));
+    f->staging_bytes = cap;
+    return HC_OK;
+}
+
+static size_t layout_bytes(long long n, int layout) {
+    return layout == HC_LAYOUT_AOS6_F64 ? n * 6 * sizeof(double)
+         : layout == HC_LAYOUT_SOA5_F64 ? n * 5 * sizeof(double) : n * 5 * sizeof(float);
+}
+
+// buffer holding a slot's current state
+static int state_buf(FusedSet* f, int slot) {
+    if (!f->rotates) return 0;
+    int rot = 0;
+    cudaMemcpyAsync(&rot, &f->d_ctl[slot].rot, sizeof(int), cudaMemcpyDeviceToHost, f->stream);
+    cudaStreamSynchronize(f->stream);
+    return rot ? f->rot_buf : 0;
+}
+
+int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int reset) {
+    Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
+    size_t const bytes = layout_bytes(S.cells, layout);
+    HC_CHECK(ensure_staging(f, bytes));
+    HC_CUDA(cudaMemcpyAsync(f->staging, host, bytes, cudaMemcpyHostToDevice, f->stream));
+    int const b = state_buf(f, slot);
+    A->xfer(f->d_inst, slot, b, f->staging, layout, 0, f->stream);
+    if (reset) A->constrain(f->d_inst, slot, b, f->stream);
+    A->fill_ghosts(f->d_inst, slot, b, f->stream);
+    fz::k_reset_dtmin<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
+    A->calc_dt(f->d_inst, f->d_ctl, slot, b, f->stream);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int fused_get_state(FusedSet* f, int slot, void* host, int layout) {
+    Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
+    size_t const bytes = layout_bytes(S.cells, layout);
+    HC_CHECK(ensure_staging(f, bytes));
+    A->xfer(f->d_inst, slot, state_buf(f, slot), f->staging, layout, 1, f->stream);
+    HC_CUDA(cudaGetLastError());
+    HC_CUDA(cudaMemcpyAsync(host, f->staging, bytes, cudaMemcpyDeviceToHost, f->stream));
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    return HC_OK;
+}
+
+int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout, double t_end, long long max_steps) {
+    if (slot < 0 || slot >= f->max_slots || f->slots[slot].used) return fail(HC_ERR_STATE, "slot unavailable");
+    HC_CHECK(validate(f, d));
+    Slot& S = f->slots[slot];
+    S.d = d;
+    S.dim = d.dim;
+    int px, py, pz;
+    padded_dims(d, px, py, pz);
+    size_t const plane = (size_t)px * py * pz;
+    size_t const planeBytes = round_up(plane * f->esize, 256);
+    int const nb = f->plan[0].n_state_bufs, nd = f->plan[0].n_deriv_bufs;
+    S.bytes = planeBytes * 5 * (nb + nd);
+    cudaError_t e = cudaMalloc(&S.mem, S.bytes);
+    if (e != cudaSuccess) { S.mem = nullptr; return cuda_fail(e, "cudaMalloc (instance state)"); }
+    HC_CUDA(cudaMemsetAsync(S.mem, 0, S.bytes, f->stream));
+    DevInst& I = S.inst;
+    std::memset(&I, 0, sizeof(I));
+    I.dim = d.dim;
+    for (int k = 0; k < 3; ++k) I.n[k] = k < d.dim ? d.n[k] : 1;
+    S.cells = (long long)I.n[0] * I.n[1] * I.n[2];
+    I.px = px; I.py = py; I.pz = pz;
+    I.plane = (long long)(planeBytes / f->esize);
+    for (int k = 0; k < 6; ++k) I.bc[k] = d.boundary[k];
+    // grid_dx and the calcDerivFromFlux / calcFlux area factors, evaluated in
+    // double in the reference's order (fvsolver.cl:37-102, fvsolver.lua:97-111)
+    for (int k = 0; k < 3; ++k) I.grid_dx[k] = (d.maxs[k] - d.mins[k]) / (double)(k < d.dim ? d.n[k] : 1);
+    double volume = 1.;
+    for (int k = 0; k < d.dim; ++k) volume = volume * I.grid_dx[k];
+    for (int side = 0; side < 3; ++side) {
+        double area = 1.;
+        for (int k = 0; k < d.dim; ++k) if (k != side) area = area * I.grid_dx[k];
+        I.zeroFlux[side] = area <= 1e-7;
+        if (volume > 1e-7) {
+            double const invVolume = 1. / volume;
+            double a = area;
+            if (a <= 1e-7) a = 0.;
+            a *= invVolume;
+            I.area[side] = a;
+            I.skipDeriv[side] = 0;
+        } else {
+            I.area[side] = 0.;
+            I.skipDeriv[side] = 1;
+        }
+    }
+    I.gamma = d.gamma;
+    I.rhoMin = d.rho_min;
+    I.PMin = d.p_min;
+    I.cfl = d.cfl;
+    I.fixed_dt = d.fixed_dt;
+    I.t_end = t_end;
+    I.max_steps = max_steps;
+    char* p = (char*)S.mem;
+    for (int b = 0; b < nb; ++b, p += planeBytes * 5) I.buf[b] = p;
+    for (int b = 0; b < nd; ++b, p += planeBytes * 5) I.dbuf[b] = p;
+    S.used = true;
+    HC_CUDA(cudaMemcpyAsync(f->d_inst + slot, &I, sizeof(DevInst), cudaMemcpyHostToDevice, f->stream));
+    DevCtl c;
+    std::memset(&c, 0, sizeof(c));
+    c.dtmin[0] = c.dtmin[1] = kInfBits;
+    c.active = 1;
+    HC_CUDA(cudaMemcpyAsync(f->d_ctl + slot, &c, sizeof(DevCtl), cudaMemcpyHostToDevice, f->stream));
+    int r = encode_maps(f, slot);
+    if (r == HC_OK && host) r = fused_set_state(f, slot, host, layout, 1);
+    if (r != HC_OK) {
+        fused_remove(f, slot);
+        return r;
+    }
+    f->items_dirty = true;
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    return HC_OK;
+}
+
+int fused_remove(FusedSet* f, int slot) {
+    if (slot < 0 || slot >= f->max_slots) return fail(HC_ERR_INVALID, "slot");
+    Slot& S = f->slots[slot];
+    if (!S.used) return HC_OK;
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    cudaFree(S.mem);
+    S.mem = nullptr;
+    S.used = false;
+    DevCtl c;
+    std::memset(&c, 0, sizeof(c));
+    HC_CUDA(cudaMemcpyAsync(f->d_ctl + slot, &c, sizeof(DevCtl), cudaMemcpyHostToDevice, f->stream));
+    f->items_dirty = true;
+    return HC_OK;
+}
+
+// Rebuilds the per-dimension (slot, tile) work lists.  Items are ordered by
+// slot, then z, y, x tile, so consecutive CTAs work on neighbouring tiles and
+// share halo rows in L2.
+static int rebuild_items(FusedSet* f) {
+    if (!f->items_dirty) return HC_OK;
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    HC_CUDA(cudaMemcpy(f->h_ctl, f->d_ctl, sizeof(DevCtl) * f->max_slots, cudaMemcpyDeviceToHost));
+    std::vector<int4> items[3];
+    for (int s = 0; s < f->max_slots; ++s) {
+        const Slot& S = f->slots[s];
+        if (!S.used || !f->h_ctl[s].active) continue;
+        const StageLauncher* L = f->launcher[S.dim - 1];
+        int const ntx = (S.inst.n[0] + L->tx - 1) / L->tx;
+        int const nty = S.dim > 1 ? (S.inst.n[1] + L->ty - 1) / L->ty : 1;
+        int const ntz = S.dim > 2 ? (S.inst.n[2] + L->tz - 1) / L->tz : 1;
+        for (int z = 0; z < ntz; ++z)
+            for (int y = 0; y < nty; ++y)
+                for (int x = 0; x < ntx; ++x) items[S.dim - 1].push_back(make_int4(s, x, y, z));
+    }
+    int mask = 0;
+    for (int d = 0; d < 3; ++d) {
+        size_t const n = items[d].size();
+        if (n) mask |= 1 << d;
+        if (n > f->items_cap[d]) {
+            cudaFree(f->d_items[d]);
+            f->d_items[d] = nullptr;
+            size_t const cap = std::max(n * 2, (size_t)1024);
+            HC_CUDA(cudaMalloc(&f->d_items[d], cap * sizeof(int4)));
+            f->items_cap[d] = cap;
+            f->graph_valid = false;
+        }
+        if (n) HC_CUDA(cudaMemcpyAsync(f->d_items[d], items[d].data(), n * sizeof(int4), cudaMemcpyHostToDevice, f->stream));
+        f->h_nitems[d] = (int)n;
+    }
+    HC_CUDA(cudaMemcpyAsync(f->d_nitems, f->h_nitems, sizeof(int) * 3, cudaMemcpyHostToDevice, f->stream));
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    if (mask != f->graph_dims_mask) f->graph_valid = false;
+    f->graph_dims_mask = mask;
+    f->items_dirty = false;
+    return HC_OK;
+}
+
+static void fill_stage(StageDev& sd, const StagePlan& sp) {
+    std::memset(&sd, 0, sizeof(sd));
+    sd.in_buf = sp.in_buf;
+    sd.out_buf = sp.out_buf;
+    sd.n_alpha = sp.n_alpha;
+    for (int k = 0; k < sp.n_alpha; ++k) { sd.alpha_buf[k] = sp.alpha[k].buf; sd.alpha[k] = sp.alpha[k].coef; }
+    sd.n_beta = sp.n_beta;
+    for (int k = 0; k < sp.n_beta; ++k) { sd.beta_buf[k] = sp.beta[k].buf; sd.beta[k] = sp.beta[k].coef; }
+    sd.beta_cur = sp.beta_cur;
+    sd.store_deriv = sp.store_deriv;
+    sd.last = sp.last;
+}
+
+// Launches the stages of one step with plan p (k_begin / k_set_dt around it
+// are the caller's).
+static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
+    for (int s = 0; s < P.n_stages; ++s) {
+        for (int d = 0; d < 3; ++d) {
+            if (!(dims_mask & (1 << d))) continue;
+            StageArgs a;
+            a.inst = f->d_inst;
+            a.ctl = f->d_ctl;
+            a.tmaps = f->d_tmaps;
+            a.items = f->d_items[d];
+            a.nitems = f->d_nitems + d;
+            a.err = f->d_err;
+            a.rot_buf = f->rot_buf;
+            fill_stage(a.st, P.stage[s]);
+            f->launcher[d]->launch(a, f->sch.slope_limiter, f->sch.flux_limiter, f->grid[d], f->stream);
+        }
+    }
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+static int launch_step(FusedSet* f, int dims_mask) {
+    unsigned const g = (unsigned)((f->max_slots + 127) / 128);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates);
+    return launch_stages(f, f->plan[0], dims_mask);
+}
+
+static int capture_graph(FusedSet* f) {
+    if (f->graph) { cudaGraphExecDestroy(f->graph); f->graph = nullptr; }
+    cudaGraph_t g;
+    HC_CUDA(cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal));
+    int r = launch_step(f, f->graph_dims_mask);
+    cudaError_t e = cudaStreamEndCapture(f->stream, &g);
+    if (r != HC_OK) { if (e == cudaSuccess) cudaGraphDestroy(g); return r; }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&f->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    f->graph_valid = true;
+    return HC_OK;
+}
+
+int fused_steps(FusedSet* f, int steps) {
+    if (steps <= 0) return HC_OK;
+    HC_CHECK(rebuild_items(f));
+    if (!f->graph_dims_mask) return HC_OK;
+    if (!f->graph_valid) HC_CHECK(capture_graph(f));
+    for (int k = 0; k < steps; ++k) HC_CUDA(cudaGraphLaunch(f->graph, f->stream));
+    unsigned const g = (unsigned)((f->max_slots + 127) / 128);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int fused_step_dt(FusedSet* f, int slot, double dt) {
+    HC_CHECK(rebuild_items(f));
+    const Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, slot, dt, 1, f->rotates);
+    HC_CHECK(launch_stages(f, f->plan[0], 1 << (S.dim - 1)));
+    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, slot, dt, 0, f->rotates);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int fused_calc_dt(FusedSet* f, int slot, double* dt) {
+    const Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    if (S.d.fixed_dt > 0) { *dt = S.d.fixed_dt; return HC_OK; }
+    const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
+    fz::k_reset_dtmin<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
+    A->calc_dt(f->d_inst, f->d_ctl, slot, state_buf(f, slot), f->stream);
+    HC_CUDA(cudaGetLastError());
+    HC_CUDA(cudaMemcpyAsync(f->h_ctl + slot, f->d_ctl + slot, sizeof(DevCtl), cudaMemcpyDeviceToHost, f->stream));
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    const DevCtl& c = f->h_ctl[slot];
+    double m;
+    unsigned long long const bits = c.dtmin[c.par];
+    std::memcpy(&m, &bits, sizeof(m));
+    *dt = S.d.cfl * m;
+    return HC_OK;
+}
+
+int fused_boundary(FusedSet* f, int slot) {
+    const Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    find_aux(f->sch.precision, S.dim)->fill_ghosts(f->d_inst, slot, state_buf(f, slot), f->stream);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int fused_constrain_u(FusedSet* f, int slot) {
+    const Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
+    A->constrain(f->d_inst, slot, state_buf(f, slot), f->stream);
+    A->fill_ghosts(f->d_inst, slot, state_buf(f, slot), f->stream);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int fused_slot_info(FusedSet* f, std::vector<SlotInfo>& out) {
+    HC_CUDA(cudaMemcpyAsync(f->h_ctl, f->d_ctl, sizeof(DevCtl) * f->max_slots, cudaMemcpyDeviceToHost, f->stream));
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    out.resize(f->max_slots);
+    for (int s = 0; s < f->max_slots; ++s) {
+        const DevCtl& c = f->h_ctl[s];
+        out[s].t = c.t;
+        out[s].dt = c.dt;
+        out[s].steps = c.steps;
+        out[s].active = c.active;
+        out[s].done = c.done;
+        out[s].status = c.status;
+    }
+    return HC_OK;
+}
+
+int fused_set_time(FusedSet* f, int slot, double t) {
+    HC_CUDA(cudaMemcpyAsync(&f->d_ctl[slot].t, &t, sizeof(double), cudaMemcpyHostToDevice, f->stream));
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    return HC_OK;
+}
+
+int fused_set_limits(FusedSet* f, int slot, double t_end, long long max_steps) {
+    Slot& S = f->slots[slot];
+    S.inst.t_end = t_end;
+    S.inst.max_steps = max_steps;
+    HC_CUDA(cudaMemcpyAsync(&f->d_inst[slot].t_end, &t_end, sizeof(double), cudaMemcpyHostToDevice, f->stream));
+    HC_CUDA(cudaMemcpyAsync(&f->d_inst[slot].max_steps, &max_steps, sizeof(long long), cudaMemcpyHostToDevice, f->stream));
+    int const one = 1, zero = 0;
+    HC_CUDA(cudaMemcpyAsync(&f->d_ctl[slot].active, &one, sizeof(int), cudaMemcpyHostToDevice, f->stream));
+    HC_CUDA(cudaMemcpyAsync(&f->d_ctl[slot].done, &zero, sizeof(int), cudaMemcpyHostToDevice, f->stream));
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    f->items_dirty = true;
+    return HC_OK;
+}
+
+int fused_conservation(FusedSet* f, int slot, double sums[5]) {
+    const Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    double vol = 1.;
+    for (int k = 0; k < S.dim; ++k) vol *= S.inst.grid_dx[k];
+    int const blocks = 1024;
+    find_aux(f->sch.precision, S.dim)->sums(f->d_inst, slot, state_buf(f, slot), vol, f->d_partial, blocks, f->stream);
+    HC_CUDA(cudaGetLastError());
+    std::vector<double> part(5 * blocks);
+    HC_CUDA(cudaMemcpyAsync(part.data(), f->d_partial, part.size() * sizeof(double), cudaMemcpyDeviceToHost, f->stream));
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    for (int j = 0; j < 5; ++j) {
+        double sm = 0, c = 0;
+        for (int b = 0; b < blocks; ++b) {
+            double const y = part[5 * b + j] - c;
+            double const t = sm + y;
+            c = (t - sm) - y;
+            sm = t;
+        }
+        sums[j] = sm;
+    }
+    return HC_OK;
+}
+
+int fused_stats(FusedSet* f, hc_batch_stats* st) {
+    std::vector<SlotInfo> info;
+    HC_CHECK(fused_slot_info(f, info));
+    std::memset(st, 0, sizeof(*st));
+    for (int s = 0; s < f->max_slots; ++s) {
+        if (!f->slots[s].used) continue;
+        st->occupied++;
+        st->bytes_in_use += f->slots[s].bytes;
+        if (info[s].active) { st->active++; st->cells += f->slots[s].cells; }
+    }
+    st->tiles = (long long)f->h_nitems[0] + f->h_nitems[1] + f->h_nitems[2];
+    return HC_OK;
+}
+
+int fused_sync(FusedSet* f) {
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    int err = 0;
+    HC_CUDA(cudaMemcpy(&err, f->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err & DEV_TIMEOUT) return fail(HC_ERR_TIMEOUT, "a bounded wait in the stage kernel ran out");
+    return HC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// autotuner: time the first stage of the plan for each tile-shape candidate
+// on the current work list and keep the fastest per dimension
+// ---------------------------------------------------------------------------
+
+static std::string tune_key(const FusedSet* f, int dim, long long cells) {
+    int bucket = 0;
+    while ((1ll << (bucket + 1)) <= cells) ++bucket;
+    std::ostringstream o;
+    o << "p" << f->sch.precision << "_d" << dim << "_plm" << (f->sch.recon == HC_RECON_PLM_CONS) << "_lim"
+      << (f->sch.flux_limiter > 0) << "_c" << bucket;
+    return o.str();
+}
+
+static void reencode_all(FusedSet* f, int dim) {
+    for (int s = 0; s < f->max_slots; ++s)
+        if (f->slots[s].used && f->slots[s].dim == dim) encode_maps(f, s);
+}
+
+int fused_autotune(FusedSet* f, const char* cache_path) {
+    std::map<std::string, int> cache;
+    if (cache_path) {
+        std::ifstream in(cache_path);
+        std::string k;
+        int v;
+        while (in >> k >> v) cache[k] = v;
+    }
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    for (int dim = 1; dim <= 3; ++dim) {
+        long long cells = 0;
+        for (const Slot& S : f->slots) if (S.used && S.dim == dim) cells += S.cells;
+        if (!cells) continue;
+        std::string const key = tune_key(f, dim, cells);
+        auto it = cache.find(key);
+        if (it != cache.end() && find_launcher(f->sch, dim, it->second)) {
+            HC_CHECK(set_launcher(f, dim, it->second));
+            reencode_all(f, dim);
+            f->items_dirty = true;
+            f->graph_valid = false;
+            continue;
+        }
+        int best = 0;
+        float bestMs = 1e30f;
+        for (int v = 0; v < 16; ++v) {
+            if (!find_launcher(f->sch, dim, v)) continue;
+            HC_CHECK(set_launcher(f, dim, v));
+            reencode_all(f, dim);
+            f->items_dirty = true;
+            HC_CHECK(rebuild_items(f));
+            unsigned const g = (unsigned)((f->max_slots + 127) / 128);
+            fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1);
+            StagePlan sp = f->plan[0].stage[0];
+            sp.last = 0;   // no dt atomics while timing
+            IntegratorPlan one;
+            std::memset(&one, 0, sizeof(one));
+            one.n_stages = 1;
+            one.stage[0] = sp;
+            HC_CHECK(launch_stages(f, one, 1 << (dim - 1)));   // warm-up
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            cudaEventRecord(e0, f->stream);
+            int const reps = 5;
+            for (int r = 0; r < reps; ++r) HC_CHECK(launch_stages(f, one, 1 << (dim - 1)));
+            cudaEventRecord(e1, f->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0);
+            HC_CUDA(cudaStreamSynchronize(f->stream));
+            if (ms < bestMs) { bestMs = ms; best = v; }
+        }
+        HC_CHECK(set_launcher(f, dim, best));
+        reencode_all(f, dim);
+        f->items_dirty = true;
+        f->graph_valid = false;
+        cache[key] = best;
+    }
+    HC_CHECK(rebuild_items(f));
+    if (cache_path) {
+        std::ofstream out(cache_path);
+        for (auto& kv : cache) out << kv.first << " " << kv.second << "\n";
+    }
+    return fused_sync(f);
+}
+
+int fused_variant(const FusedSet* f, int dim) { return f->launcher[dim - 1] ? f->launcher[dim - 1]->variant : -1; }
+
+}  // namespace hc
+
+namespace hc {
+namespace fz {
+void register_f32_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f64_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+
+void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& aux) {
+    register_f32_d1(st, aux);
+    register_f32_d2(st, aux);
+    register_f32_d3(st, aux);
+    register_f64_d1(st, aux);
+    register_f64_d2(st, aux);
+    register_f64_d3(st, aux);
+}
+}  // namespace fz
+}  // namespace hc

@@ -1,0 +1,67 @@
+// hc_fused_inst.cuh -- instantiation helpers: each translation unit that
+// includes this header compiles a set of stage-kernel configurations and
+// registers their launchers.
+#pragma once
+
+#include "hc_fused.cuh"
+
+namespace hc {
+namespace fz {
+
+template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM>
+void add_stage(std::vector<StageLauncher>& v) {
+    using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
+    StageLauncher sl;
+    sl.precision = PREC;
+    sl.dim = DIM;
+    sl.plm = PLM;
+    sl.lim = LIM;
+    sl.variant = VAR;
+    sl.tx = TX;
+    sl.ty = TY;
+    sl.tz = TZ;
+    sl.nthreads = NT;
+    sl.smem = Cfg::SMEM;
+    sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
+        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+    };
+    sl.occupancy = []() -> int {
+        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM>;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NT, Cfg::SMEM) != cudaSuccess) return -1;
+        return n;
+    };
+    v.push_back(sl);
+}
+
+inline unsigned aux_blocks(long long n) {
+    long long b = (n + 255) / 256;
+    return (unsigned)(b < 1 ? 1 : (b > 4096 ? 4096 : b));
+}
+
+template <typename T, int PREC, int DIM, bool EXACT>
+void add_aux(std::vector<AuxLauncher>& v) {
+    AuxLauncher a;
+    a.precision = PREC;
+    a.dim = DIM;
+    a.fill_ghosts = [](const DevInst* inst, int slot, int buf, cudaStream_t s) {
+        k_fill_ghosts<T, DIM><<<1024, 256, 0, s>>>(inst, slot, buf);
+    };
+    a.constrain = [](const DevInst* inst, int slot, int buf, cudaStream_t s) {
+        k_constrain<T, DIM, EXACT><<<1024, 256, 0, s>>>(inst, slot, buf);
+    };
+    a.calc_dt = [](const DevInst* inst, DevCtl* ctl, int slot, int buf, cudaStream_t s) {
+        k_calc_dt<T, DIM, EXACT><<<1024, 256, 0, s>>>(inst, ctl, slot, buf);
+    };
+    a.xfer = [](const DevInst* inst, int slot, int buf, void* staging, int layout, int dir, cudaStream_t s) {
+        k_xfer<T, DIM><<<1024, 256, 0, s>>>(inst, slot, buf, staging, layout, dir);
+    };
+    a.sums = [](const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s) {
+        k_sums<T, DIM><<<blocks, 256, 0, s>>>(inst, slot, buf, vol, partial);
+    };
+    v.push_back(a);
+}
+
+}  // namespace fz
+}  // namespace hc

@@ -1,0 +1,141 @@
+// hc_internal.h -- shared definitions of libhydrocuda (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include "../../include/hydrocuda.h"
+
+namespace hc {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define HC_CUDA(call)                                                          \
+    do {                                                                       \
+        cudaError_t hc_e_ = (call);                                            \
+        if (hc_e_ != cudaSuccess) return ::hc::cuda_fail(hc_e_, #call);        \
+    } while (0)
+
+#define HC_CHECK(call)                                                         \
+    do {                                                                       \
+        int hc_r_ = (call);                                                    \
+        if (hc_r_ != HC_OK) return hc_r_;                                      \
+    } while (0)
+
+// Device error flags written by kernels (bounded waits, non-finite results).
+enum DeviceStatus : int {
+    DEV_OK = 0,
+    DEV_NONFINITE = 1,
+    DEV_TIMEOUT = 2,
+};
+
+// ---------------------------------------------------------------------------
+// Runge-Kutta tables (hydro/int/all.lua:10-155); index 0 = forward Euler.
+// ---------------------------------------------------------------------------
+
+struct RKTable {
+    int order;            // number of stages (forward Euler: 1)
+    double alpha[4][4];   // alpha[i-1][k-1]: u^(i) = sum_k alpha u^(k) + dt beta L(u^(k))
+    double beta[4][4];
+};
+const RKTable& rk_table(int integrator);
+
+// The stage plan turns a table into fused stage launches with buffer reuse.
+struct StageTerm { int buf; double coef; };
+struct StagePlan {
+    int in_buf;                   // u^(i-1), read with halo
+    int out_buf;                  // u^(i)
+    int n_alpha;                  // alpha terms, k ascending
+    StageTerm alpha[4];           // buf = state buffer index (may equal in_buf)
+    int n_beta;                   // stored-derivative terms, k ascending (all k < i-1)
+    StageTerm beta[4];            // coef = beta (multiplied by the instance dt on device)
+    double beta_cur;              // coefficient of L(u^(i-1)) (0 if unused)
+    int store_deriv;              // derivative buffer to store L(u^(i-1)) into, or -1
+    int last;                     // final stage: also computes the next CFL dt
+};
+struct IntegratorPlan {
+    int n_stages;
+    int n_state_bufs;             // state buffers (buffer 0 holds u^n at step start)
+    int n_deriv_bufs;
+    int result_buf;               // buffer holding u^{n+1} after the step
+    StagePlan stage[4];
+};
+// Builds the plan; buffers are reused when a stage's output can overwrite a
+// state that is only read pointwise from then on.  The current state rotates:
+// a step starts from state buffer `start` and ends in plan.result_buf(start).
+IntegratorPlan make_plan(int integrator);
+
+// ---------------------------------------------------------------------------
+// plain FP64 form (hc_plain.cu)
+// ---------------------------------------------------------------------------
+
+struct PlainParams {
+    int dim;
+    int gs[3];            // gridSize with ghosts
+    int stepsize[3];
+    long long numCells;
+    double grid_dx[3];
+    int bc[6];
+    int fluxLimiter, recon, slopeLimiter;
+    double gamma, rhoMin, PMin;
+};
+
+struct PlainSolver;   // defined in hc_plain.cu
+int plain_create(const hc_solver_desc& d, cudaStream_t stream, PlainSolver** out);
+void plain_destroy(PlainSolver* p);
+int plain_set_full(PlainSolver* p, const double* host_aos6);
+int plain_get_full(PlainSolver* p, double* host_aos6);
+int plain_set_interior(PlainSolver* p, const void* host, int layout);
+int plain_get_interior(PlainSolver* p, void* host, int layout);
+int plain_boundary(PlainSolver* p);
+int plain_constrain_u(PlainSolver* p);
+int plain_calc_dt(PlainSolver* p, double cfl, double fixed_dt, double* dt);
+int plain_step(PlainSolver* p, int integrator, double dt);
+int plain_conservation(PlainSolver* p, double sums[5]);
+long long plain_num_cells(const PlainSolver* p);
+
+// ---------------------------------------------------------------------------
+// fused form (hc_fused.cu): a set of instances advanced together
+// ---------------------------------------------------------------------------
+
+struct FusedSet;      // defined in hc_fused.cu
+struct FusedScheme {
+    int precision;     // HC_F32_FUSED or HC_F64_FUSED
+    int flux_limiter, recon, slope_limiter, integrator;
+};
+int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, FusedSet** out);
+void fused_destroy(FusedSet* f);
+// bytes an instance of this shape holds on the device
+size_t fused_instance_bytes(const FusedSet* f, const hc_solver_desc& d);
+int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout,
+              double t_end, long long max_steps);
+int fused_remove(FusedSet* f, int slot);
+int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int reset);
+int fused_get_state(FusedSet* f, int slot, void* host, int layout);
+// Runs `steps` updates of every live instance (device-side completion tests).
+int fused_steps(FusedSet* f, int steps);
+// One update of the given slot's instance with an explicit dt (-1: CFL dt).
+int fused_step_dt(FusedSet* f, int slot, double dt);
+int fused_calc_dt(FusedSet* f, int slot, double* dt);
+int fused_boundary(FusedSet* f, int slot);
+int fused_constrain_u(FusedSet* f, int slot);
+struct SlotInfo { double t; double dt; long long steps; int active; int done; int status; };
+int fused_slot_info(FusedSet* f, std::vector<SlotInfo>& out);
+int fused_set_time(FusedSet* f, int slot, double t);
+int fused_set_limits(FusedSet* f, int slot, double t_end, long long max_steps);
+int fused_variant(const FusedSet* f, int dim);
+int fused_conservation(FusedSet* f, int slot, double sums[5]);
+int fused_stats(FusedSet* f, hc_batch_stats* st);
+int fused_autotune(FusedSet* f, const char* cache_path);
+int fused_sync(FusedSet* f);
+
+}  // namespace hc

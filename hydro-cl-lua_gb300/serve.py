@@ -1,0 +1,157 @@
+"""Continuous-batching request loop over hc_batch (host side).
+
+Requests (Euler solves of any dimension and size, each with its own end time)
+arrive over time.  The loop admits every arrived request it can (FIFO) against
+the batch's HBM budget and slot table, advances all live solves together with
+``hc_batch_step`` (each with its own CFL dt, on the device), and as solves
+finish it fetches their states, retires their slots (returning their bytes to
+the budget) and records time-to-solution.  Requests that arrive while others
+are on the GPU are admitted as soon as memory and a slot free up, so their
+work overlaps on the device with the solves already running.
+
+The reference has no serving layer: each hydro-cl-lua App steps its solvers in
+its own loop (hydro/app.lua:1573-1750).  One request here is one App run to
+exitTime (the exit test precedes each update, so the last update overshoots).
+"""
+import collections
+import time
+
+import numpy as np
+
+import hydrocuda
+
+
+class Request:
+    __slots__ = ("arrival", "args", "cons", "t_end", "tag", "admitted", "finished", "steps", "t", "status", "result")
+
+    def __init__(self, arrival, args, cons, t_end, tag):
+        self.arrival = float(arrival)
+        self.args = args
+        self.cons = cons
+        self.t_end = float(t_end)
+        self.tag = int(tag)
+        self.admitted = None
+        self.finished = None
+        self.steps = 0
+        self.t = 0.0
+        self.status = None
+        self.result = None
+
+
+class Server:
+    """Drives one hc_batch with a stream of requests.
+
+    steps_per_tick: updates per hc_batch_step call between admission / poll
+    passes (larger values amortise host round trips, smaller ones admit and
+    retire sooner).  keep_results: fetch the final state of every solve.
+    """
+
+    def __init__(self, batch, steps_per_tick=8, keep_results=True, result_layout="aos6"):
+        self.batch = batch
+        self.steps_per_tick = int(steps_per_tick)
+        self.keep_results = keep_results
+        self.result_layout = result_layout
+        self.by_tag = {}
+        self.slot_of = {}
+        self.ticks = 0
+        self.cell_updates = 0
+
+    def run(self, requests, clock=None, sleep=None, max_wall=None):
+        """Serves `requests` (sorted by arrival time, seconds from start).
+
+        clock(): seconds since start; defaults to the wall clock.  Returns the
+        list of finished requests with latency fields filled in.
+        """
+        t0 = time.perf_counter()
+        clock = clock or (lambda: time.perf_counter() - t0)
+        sleep = sleep or time.sleep
+        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        live = 0
+        done = []
+        cells_of = {}
+        while pending or live:
+            now = clock()
+            if max_wall is not None and now > max_wall:
+                break
+            # admit every arrived request that fits
+            while pending and pending[0].arrival <= now:
+                r = pending[0]
+                slot = self.batch.try_admit(r.args, r.cons, r.t_end, tag=r.tag)
+                if slot is None:
+                    if live == 0:
+                        raise RuntimeError("request %d does not fit an empty batch" % r.tag)
+                    break
+                pending.popleft()
+                r.admitted = clock()
+                r.cons = None
+                self.by_tag[r.tag] = r
+                self.slot_of[r.tag] = slot
+                d = self.batch.slot_desc[slot]
+                cells_of[r.tag] = hydrocuda.interior_count(d)
+                live += 1
+            if live:
+                self.batch.step(self.steps_per_tick)
+                self.ticks += 1
+                for ev in self.batch.poll():
+                    r = self.by_tag.pop(ev["tag"])
+                    slot = self.slot_of.pop(r.tag)
+                    r.steps = ev["steps"]
+                    r.t = ev["t"]
+                    r.status = ev["status"]
+                    if self.keep_results:
+                        r.result = self.batch.fetch(slot, self.result_layout)
+                    self.batch.retire(slot)
+                    r.finished = clock()
+                    self.cell_updates += r.steps * cells_of.pop(r.tag)
+                    live -= 1
+                    done.append(r)
+            elif pending:
+                sleep(max(0.0, pending[0].arrival - clock()))
+        return done
+
+
+def latency_summary(done):
+    lat = np.array([r.finished - r.arrival for r in done])
+    return {
+        "count": int(lat.size),
+        "p50_s": float(np.percentile(lat, 50)) if lat.size else None,
+        "p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+        "mean_s": float(lat.mean()) if lat.size else None,
+    }
+
+
+def synthetic_stream(count, rate_hz, seed=5, scale=1.0, gamma=1.4):
+    """Poisson arrivals (mean rate_hz) of 1D / 2D / 3D Euler solves.
+
+    40 % 1D with N ~ logU[512, 65536], 45 % 2D with N ~ logU[128, 1024],
+    15 % 3D with N ~ logU[64, 192] (N scaled by `scale` for reduced runs);
+    the initial state is uniformly one of Sod (along x), blast, quadrant;
+    t_end ~ U(0.05, 0.2).  Scheme: plm cons + minmod, Runge-Kutta 2, CFL 0.3.
+    """
+    rng = hydrocuda.SplitMix64(seed)
+    t = 0.0
+    out = []
+    for tag in range(count):
+        t += -np.log(1.0 - rng.uniform()) / rate_hz
+        u = rng.uniform()
+        if u < .40:
+            dim, lo, hi = 1, 512, 65536
+        elif u < .85:
+            dim, lo, hi = 2, 128, 1024
+        else:
+            dim, lo, hi = 3, 64, 192
+        n = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi))) * scale))
+        n = max(n, 8)
+        kind = int(rng.uniform() * 3)
+        t_end = rng.uniform(0.05, 0.2)
+        args = dict(dim=dim, gridSize=[n] * dim, mins=[-1, -1, -1], maxs=[1, 1, 1], boundary="freeflow",
+                    usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2", cfl=.3,
+                    eqnArgs={"heatCapacityRatio": gamma})
+        if kind == 0 or dim == 1 and kind == 2:
+            cons = hydrocuda.sod_state(args)
+        elif kind == 1:
+            cons = hydrocuda.blast_state(args)
+        else:
+            cons = hydrocuda.quadrant_state(args, hydrocuda.random_quadrants(rng)) if dim == 2 else hydrocuda.blast_state(args)
+        out.append(Request(t, args, cons, t_end, tag))
+    return out

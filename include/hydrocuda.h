@@ -1,0 +1,244 @@
+/*
+ * hydrocuda.h -- C ABI of libhydrocuda.so, a GB300 (sm_103a) implementation of
+ * hydro-cl-lua's finite-volume Euler update: ghost-cell boundary fill, "plm
+ * cons" reconstruction with the reference's slope limiters, the Roe flux on
+ * the Euler eigen-decomposition (optionally flux-limited), calcDerivFromFlux,
+ * the CFL calcDT min-reduction, constrainU, and the explicit forward-Euler and
+ * Runge-Kutta integrators.
+ *
+ * Plain C99; no callbacks; no library types in the signatures.  Every entry
+ * point returns 0 (HC_OK) or a negative HC_ERR_* code; hc_last_error() gives a
+ * thread-local message for the last failure on the calling thread.  The
+ * caller owns every host array passed in; nothing is retained after return.
+ * Device memory is owned by the library behind opaque handles.  A handle is
+ * used from one host thread at a time.
+ *
+ * Reference interfaces replaced (paths within hydro-cl-lua):
+ *   solver construction   hydro/solver/solverbase.lua:324-398, gridsolver.lua:60-136,
+ *                         fvsolver.lua:28-31, 201-211 (the solver args table)
+ *   resetState            hydro/solver/solverbase.lua:2094-2114
+ *   boundary              hydro/solver/gridsolver.lua:1316-1320 (kernels 1070-1213)
+ *   constrainU            hydro/solver/solverbase.lua:2116-2128, hydro/eqn/euler.cl:697-717
+ *   calcDT                hydro/solver/solverbase.lua:3004-3024, hydro/eqn/cl/calcDT.cl:38-73
+ *   step / integrate      hydro/solver/solverbase.lua:3193-3238, hydro/int/fe.lua:33-49,
+ *                         hydro/int/rk.lua:98-218
+ *   update                hydro/solver/solverbase.lua:3026-3190
+ *   App exit loop         hydro/app.lua:1573-1600 (t >= exitTime checked before stepping)
+ *   UBuf readback         hydro/solver/gridsolver.lua:1337-1366 (UBufObj:toCPU)
+ */
+#ifndef HYDROCUDA_H
+#define HYDROCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HC_VERSION_MAJOR 0
+#define HC_VERSION_MINOR 3
+
+/* return codes */
+#define HC_OK               0
+#define HC_ERR_INVALID     -1   /* bad argument or unsupported option combination */
+#define HC_ERR_CUDA        -2   /* a CUDA runtime call failed */
+#define HC_ERR_NOMEM       -3   /* device or host allocation failed */
+#define HC_ERR_BUDGET      -4   /* admission would exceed the batch's HBM budget */
+#define HC_ERR_NO_SLOT     -5   /* every batch slot is in use */
+#define HC_ERR_NONFINITE   -6   /* a solve produced a non-finite dt or state */
+#define HC_ERR_TIMEOUT     -7   /* a bounded device wait ran out */
+#define HC_ERR_STATE       -8   /* call not valid in the handle's current state */
+
+/* boundary names (gridsolver.lua:617-780) */
+#define HC_BOUNDARY_NONE      0
+#define HC_BOUNDARY_PERIODIC  1
+#define HC_BOUNDARY_MIRROR    2
+#define HC_BOUNDARY_FREEFLOW  3
+
+/* limiter table, in the order of hydro/app.lua:614-635 (reference index - 1);
+ * HC_LIMITER_DONOR_CELL as flux limiter means "no flux limiter" */
+#define HC_LIMITER_DONOR_CELL        0
+#define HC_LIMITER_LAX_WENDROFF      1
+#define HC_LIMITER_BEAM_WARMING      2
+#define HC_LIMITER_FROMM             3
+#define HC_LIMITER_CHARM             4
+#define HC_LIMITER_HCUS              5
+#define HC_LIMITER_HQUICK            6
+#define HC_LIMITER_KOREN             7
+#define HC_LIMITER_MINMOD            8
+#define HC_LIMITER_OSHKER            9
+#define HC_LIMITER_OSPRE            10
+#define HC_LIMITER_SMART            11
+#define HC_LIMITER_SWEBY            12
+#define HC_LIMITER_UMIST            13
+#define HC_LIMITER_VAN_ALBADA_1     14
+#define HC_LIMITER_VAN_ALBADA_2     15
+#define HC_LIMITER_VAN_LEER         16
+#define HC_LIMITER_MONOTIZED_CENTRAL 17
+#define HC_LIMITER_SUPERBEE         18
+#define HC_LIMITER_BARTH_JESPERSEN  19
+#define HC_NUM_LIMITERS             20
+
+/* usePLM (hydro/solver/plm.cl) */
+#define HC_RECON_NONE                0   /* usePLM = nil: interface states are the cell states */
+#define HC_RECON_PIECEWISE_CONSTANT  1   /* "piecewise constant" */
+#define HC_RECON_PLM_CONS            2   /* "plm cons" */
+
+/* explicit integrators (hydro/int/all.lua) */
+#define HC_INT_FORWARD_EULER   0
+#define HC_INT_RK2             1   /* "Runge-Kutta 2" (midpoint) */
+#define HC_INT_RK2_HEUN        2
+#define HC_INT_RK2_RALSTON     3
+#define HC_INT_RK3             4
+#define HC_INT_RK4             5
+#define HC_INT_RK4_38          6   /* "Runge-Kutta 4, 3/8ths rule" */
+#define HC_INT_RK2_TVD         7
+#define HC_INT_RK2_NONTVD      8
+#define HC_INT_RK3_TVD         9
+#define HC_INT_RK4_TVD        10
+#define HC_INT_RK4_NONTVD     11
+#define HC_NUM_INTEGRATORS    12
+
+/* arithmetic forms */
+#define HC_F64_PLAIN   0   /* kernel-for-kernel FP64 form of the reference, array-of-structs */
+#define HC_F64_FUSED   1   /* fused stage kernel, structure-of-arrays, FP64 */
+#define HC_F32_FUSED   2   /* fused stage kernel, FP32 bulk; FP64 dt reduction, time and sums */
+
+/* host array layouts for state I/O.  Cells in x-fastest order.
+ * AOS6_F64: cons_t {rho, m.x, m.y, m.z, ETotal, ePot} as 6 doubles per cell
+ * SOA5_F64: 5 planes of doubles (rho, m.x, m.y, m.z, ETotal); ePot is 0
+ * SOA5_F32: 5 planes of floats */
+#define HC_LAYOUT_AOS6_F64  0
+#define HC_LAYOUT_SOA5_F64  1
+#define HC_LAYOUT_SOA5_F32  2
+
+/* The solver args table (solverbase.lua:324-338; gridsolver.lua:98-104) as a struct. */
+typedef struct hc_solver_desc {
+    int    dim;              /* 1, 2 or 3 */
+    int    n[3];             /* gridSize without ghosts; unused axes ignored */
+    double mins[3];          /* domain; unused axes keep their extent for grid_dx */
+    double maxs[3];
+    int    boundary[6];      /* xmin xmax ymin ymax zmin zmax, HC_BOUNDARY_* */
+    int    flux_limiter;     /* HC_LIMITER_* (Roe flux limiter; donor cell = off) */
+    int    recon;            /* HC_RECON_* */
+    int    slope_limiter;    /* HC_LIMITER_* (used by PLM) */
+    int    integrator;       /* HC_INT_* */
+    int    precision;        /* HC_F64_PLAIN | HC_F64_FUSED | HC_F32_FUSED */
+    double gamma;            /* heatCapacityRatio, reference default 7/5 */
+    double rho_min;          /* reference default 1e-7 */
+    double p_min;            /* reference default 1e-7 */
+    double cfl;              /* reference default .5 */
+    double fixed_dt;         /* > 0: useFixedDT with this dt; <= 0: CFL dt */
+} hc_solver_desc;
+
+typedef struct hc_context hc_context;
+typedef struct hc_solver  hc_solver;
+typedef struct hc_batch   hc_batch;
+
+/* ---- library / context ------------------------------------------------ */
+
+/* Version string "major.minor". */
+const char* hc_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char* hc_last_error(void);
+/* Number of visible CUDA devices. */
+int hc_device_count(int* count);
+/* One context per device; owns the streams the handles below use. */
+int hc_context_create(int device, hc_context** out);
+int hc_context_destroy(hc_context* ctx);
+/* Pinned host memory for fast state transfers (optional). */
+int hc_host_alloc(size_t bytes, void** out);
+int hc_host_free(void* p);
+
+/* ---- single solver (FiniteVolumeSolver with flux='roe', eqn='euler') ---- */
+
+/* Validates the descriptor and allocates device state.  Replaces the
+ * solver class construction, solverbase.lua:351-398. */
+int hc_solver_create(hc_context* ctx, const hc_solver_desc* desc, hc_solver** out);
+int hc_solver_destroy(hc_solver* s);
+/* resetState after applyInitCond (solverbase.lua:2094-2114): writes the
+ * interior conserved state, fills the ghosts, applies constrainU, sets t = 0. */
+int hc_solver_reset_state(hc_solver* s, const void* cons, int layout);
+/* Raw state I/O.  with_ghosts = 1 reads/writes the full grid including the
+ * numGhost = 2 layers (AOS6_F64 only); 0 the interior only. */
+int hc_solver_set_state(hc_solver* s, const void* cons, int layout, int with_ghosts);
+int hc_solver_get_state(hc_solver* s, void* cons, int layout, int with_ghosts);
+/* GridSolver:boundary() (gridsolver.lua:1316). */
+int hc_solver_boundary(hc_solver* s);
+/* SolverBase:constrainU() (solverbase.lua:2116), boundary included. */
+int hc_solver_constrain_u(hc_solver* s);
+/* SolverBase:calcDT() (solverbase.lua:3004): cfl * min over cells, or fixed_dt. */
+int hc_solver_calc_dt(hc_solver* s, double* dt);
+/* SolverBase:step(dt) (solverbase.lua:3193): one integrator step. */
+int hc_solver_step(hc_solver* s, double dt);
+/* SolverBase:update() (solverbase.lua:3026): calcDT, step, t += dt, boundary. */
+int hc_solver_update(hc_solver* s, double* dt_out);
+/* The App loop: while t < t_end and steps < max_steps, update().  The test is
+ * made before each update, so the final step overshoots t_end (app.lua:1590). */
+int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long long* steps_done);
+int hc_solver_get_time(hc_solver* s, double* t);
+int hc_solver_set_time(hc_solver* s, double t);
+/* Kahan-compensated FP64 sums of rho, m.x, m.y, m.z, ETotal times cell volume
+ * over the interior. */
+int hc_solver_conservation(hc_solver* s, double sums[5]);
+/* HC_OK, or the first error a kernel recorded (HC_ERR_NONFINITE, HC_ERR_TIMEOUT). */
+int hc_solver_status(hc_solver* s);
+
+/* ---- batched, continuously admitted solves ------------------------------ */
+
+typedef struct hc_batch_desc {
+    int    precision;        /* HC_F32_FUSED or HC_F64_FUSED */
+    int    flux_limiter;     /* shared by every instance of the batch */
+    int    recon;
+    int    slope_limiter;
+    int    integrator;
+    int    max_slots;        /* slot table size */
+    size_t hbm_budget;       /* bytes of device state the batch may hold */
+} hc_batch_desc;
+
+typedef struct hc_done {
+    int                slot;
+    int                status;   /* HC_OK or HC_ERR_NONFINITE */
+    unsigned long long tag;
+    long long          steps;
+    double             t;
+} hc_done;
+
+typedef struct hc_batch_stats {
+    int       active;            /* instances still stepping */
+    int       occupied;          /* slots holding a result or a live instance */
+    size_t    bytes_in_use;      /* device state bytes charged to the budget */
+    long long tiles;             /* tiles in the current work list */
+    long long cells;             /* interior cells of live instances */
+} hc_batch_stats;
+
+int hc_batch_create(hc_context* ctx, const hc_batch_desc* desc, hc_batch** out);
+int hc_batch_destroy(hc_batch* b);
+/* Admits one instance: validates it against the batch's shared scheme,
+ * charges its state bytes to the HBM budget (HC_ERR_BUDGET if over) and takes
+ * a free slot (HC_ERR_NO_SLOT if none), uploads the interior conserved state,
+ * applies resetState, computes its first dt.  The instance then advances with
+ * every hc_batch_step until t >= t_end or max_steps updates. */
+int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout,
+                   double t_end, long long max_steps, unsigned long long tag, int* slot);
+/* Advances every live instance by up to `steps` updates (each instance with its
+ * own CFL dt), in batched launches.  *n_active = instances still stepping. */
+int hc_batch_step(hc_batch* b, int steps, int* n_active);
+/* Lists finished instances not yet reported (at most cap). */
+int hc_batch_poll(hc_batch* b, hc_done* out, int cap, int* n_out);
+/* Copies a slot's interior state to the host. */
+int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout);
+/* Frees a slot and returns its bytes to the budget. */
+int hc_batch_retire(hc_batch* b, int slot);
+int hc_batch_stats_get(hc_batch* b, hc_batch_stats* out);
+int hc_batch_conservation(hc_batch* b, int slot, double sums[5]);
+/* Times the candidate tile shapes on the batch's current work list and keeps
+ * the fastest; reads/writes the choice from/to cache_path when not NULL. */
+int hc_batch_autotune(hc_batch* b, const char* cache_path);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYDROCUDA_H */

@@ -1,0 +1,252 @@
+"""ctypes wrapper for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+The oracle (``hydro_oracle.cpp``) is a double-precision C++ restatement of
+hydro-cl-lua's generated OpenCL kernels for the Euler / Roe / PLM / Runge-Kutta
+path.  Only the tests, the smoke check and the benchmark's CPU-baseline leg
+import this module; the product library never does.
+
+Parity anchoring: the reference itself cannot run here (no LuaJIT, no OpenCL
+CPU platform), so the restatement is pinned by the density L1 errors recorded
+in the reference's accuracy harness (``tests/test-order/schemes.lua``) and by
+the eigen-basis identities the reference uses as diagnostics
+(``hydro/solver/fvsolver.lua:396-527``); see ``tests/test_oracle_pins.py``.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
+SRC = os.path.join(HERE, "hydro_oracle.cpp")
+
+# Names in the order of the reference's limiter table (hydro/app.lua:614-635).
+LIMITERS = [
+    "donor cell", "Lax-Wendroff", "Beam-Warming", "Fromm", "CHARM", "HCUS",
+    "HQUICK", "Koren", "minmod", "Oshker", "ospre", "smart", "Sweby", "UMIST",
+    "van Albada 1", "van Albada 2", "van Leer", "monotized central",
+    "superbee", "Barth-Jespersen",
+]
+# Explicit integrators (hydro/int/all.lua), in the oracle's numbering.
+INTEGRATORS = [
+    "forward Euler", "Runge-Kutta 2", "Runge-Kutta 2 Heun",
+    "Runge-Kutta 2 Ralston", "Runge-Kutta 3", "Runge-Kutta 4",
+    "Runge-Kutta 4, 3/8ths rule", "Runge-Kutta 2, TVD",
+    "Runge-Kutta 2, non-TVD", "Runge-Kutta 3, TVD", "Runge-Kutta 4, TVD",
+    "Runge-Kutta 4, non-TVD",
+]
+BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3}
+RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2}
+
+
+def build(force=False):
+    """Compile the oracle with g++ (no FMA contraction, OpenMP)."""
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
+           "-shared", "-fPIC", SRC, "-o", tmp]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class OrDesc(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int),
+        ("n", ctypes.c_int * 3),
+        ("mins", ctypes.c_double * 3),
+        ("maxs", ctypes.c_double * 3),
+        ("boundary", ctypes.c_int * 6),
+        ("flux_limiter", ctypes.c_int),
+        ("recon", ctypes.c_int),
+        ("slope_limiter", ctypes.c_int),
+        ("integrator", ctypes.c_int),
+        ("gamma", ctypes.c_double),
+        ("rho_min", ctypes.c_double),
+        ("p_min", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("fixed_dt", ctypes.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        L = ctypes.CDLL(path)
+        vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
+        L.or_create.restype = vp
+        L.or_create.argtypes = [ctypes.POINTER(OrDesc)]
+        L.or_destroy.argtypes = [vp]
+        L.or_num_cells.restype = ctypes.c_long
+        L.or_num_cells.argtypes = [vp]
+        for name in ("or_set_state_full", "or_get_state_full", "or_reset_state", "or_get_interior"):
+            getattr(L, name).argtypes = [vp, dp]
+        L.or_boundary.argtypes = [vp]
+        L.or_constrain_u.argtypes = [vp]
+        L.or_calc_dt.restype = ctypes.c_double
+        L.or_calc_dt.argtypes = [vp]
+        L.or_step.argtypes = [vp, ctypes.c_double]
+        L.or_update.restype = ctypes.c_double
+        L.or_update.argtypes = [vp]
+        L.or_get_t.restype = ctypes.c_double
+        L.or_get_t.argtypes = [vp]
+        L.or_set_t.argtypes = [vp, ctypes.c_double]
+        L.or_run_until.restype = ctypes.c_long
+        L.or_run_until.argtypes = [vp, ctypes.c_double, ctypes.c_long]
+        L.or_calc_deriv.argtypes = [vp, ctypes.c_double, dp]
+        L.or_get_flux.argtypes = [vp, dp]
+        L.or_roe_flux.argtypes = [ctypes.POINTER(OrDesc), dp, dp, ip, dp]
+        L.or_eigen_basis.argtypes = [ctypes.POINTER(OrDesc), dp, dp, ip, dp, dp, dp]
+        L.or_limiter.restype = ctypes.c_double
+        L.or_limiter.argtypes = [ip, ctypes.c_double]
+        L.or_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_desc(cfg):
+    """Map a reference-style solver args table (a dict) onto the oracle descriptor."""
+    d = OrDesc()
+    dim = int(cfg["dim"])
+    gs = cfg["gridSize"]
+    if isinstance(gs, int):
+        gs = [gs]
+    mins = list(cfg.get("mins", [-1, -1, -1])) + [-1] * 3
+    maxs = list(cfg.get("maxs", [1, 1, 1])) + [1] * 3
+    d.dim = dim
+    for k in range(3):
+        d.n[k] = int(gs[k]) if k < dim else 1
+        d.mins[k] = float(mins[k])
+        d.maxs[k] = float(maxs[k])
+    bnd = cfg.get("boundary", {}) or {}
+    if isinstance(bnd, str):
+        bnd = {k: bnd for k in ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")}
+    for k, name in enumerate(("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")):
+        d.boundary[k] = BOUNDARIES[bnd.get(name, "freeflow")]
+    d.flux_limiter = LIMITERS.index(cfg.get("fluxLimiter", "donor cell"))
+    d.recon = RECONS[cfg.get("usePLM", None)]
+    d.slope_limiter = LIMITERS.index(cfg.get("slopeLimiter", "donor cell"))
+    d.integrator = INTEGRATORS.index(cfg.get("integrator", "forward Euler"))
+    eq = cfg.get("eqnArgs", {}) or {}
+    d.gamma = float(eq.get("heatCapacityRatio", 7.0 / 5.0))
+    d.rho_min = float(eq.get("rhoMin", 1e-7))
+    d.p_min = float(eq.get("PMin", 1e-7))
+    d.cfl = float(cfg.get("cfl", 0.5))
+    d.fixed_dt = float(cfg.get("fixedDT", 0.0) or 0.0)
+    return d
+
+
+class OracleSolver:
+    """The oracle behind the reference's solver-args vocabulary."""
+
+    def __init__(self, cfg):
+        self.cfg = dict(cfg)
+        self.desc = make_desc(cfg)
+        self.L = lib()
+        self.h = self.L.or_create(ctypes.byref(self.desc))
+        if not self.h:
+            raise ValueError("oracle rejected the configuration")
+        self.dim = self.desc.dim
+        self.n = [self.desc.n[k] for k in range(3)]
+        self.gs = [self.n[k] + 4 if k < self.dim else 1 for k in range(3)]
+        self.num_cells = int(self.L.or_num_cells(self.h))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.L.or_destroy(h)
+            self.h = None
+
+    # state I/O ---------------------------------------------------------
+    def reset_state(self, cons_interior):
+        """cons_interior: float64 array (..., 6) in x-fastest order, interior cells only."""
+        a = np.ascontiguousarray(cons_interior, dtype=np.float64).reshape(-1, 6)
+        assert a.shape[0] == self.n[0] * self.n[1] * self.n[2]
+        self.L.or_reset_state(self.h, _ptr(a))
+
+    def get_interior(self):
+        out = np.empty((self.n[0] * self.n[1] * self.n[2], 6), dtype=np.float64)
+        self.L.or_get_interior(self.h, _ptr(out))
+        return out
+
+    def get_full(self):
+        out = np.empty((self.num_cells, 6), dtype=np.float64)
+        self.L.or_get_state_full(self.h, _ptr(out))
+        return out
+
+    def set_full(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.num_cells, 6)
+        self.L.or_set_state_full(self.h, _ptr(a))
+
+    # the reference's solver verbs -----------------------------------------
+    def boundary(self):
+        self.L.or_boundary(self.h)
+
+    def constrainU(self):
+        self.L.or_constrain_u(self.h)
+
+    def calcDT(self):
+        return self.L.or_calc_dt(self.h)
+
+    def step(self, dt):
+        self.L.or_step(self.h, float(dt))
+
+    def update(self):
+        return self.L.or_update(self.h)
+
+    @property
+    def t(self):
+        return self.L.or_get_t(self.h)
+
+    @t.setter
+    def t(self, v):
+        self.L.or_set_t(self.h, float(v))
+
+    def run_until(self, t_end, max_steps=1 << 40):
+        return int(self.L.or_run_until(self.h, float(t_end), int(max_steps)))
+
+    def calc_deriv(self, dt):
+        out = np.empty((self.num_cells, 6), dtype=np.float64)
+        self.L.or_calc_deriv(self.h, float(dt), _ptr(out))
+        return out
+
+
+def roe_flux(cfg, UL, UR, side):
+    d = make_desc(cfg)
+    a = np.ascontiguousarray(UL, dtype=np.float64)
+    b = np.ascontiguousarray(UR, dtype=np.float64)
+    out = np.empty(6)
+    lib().or_roe_flux(ctypes.byref(d), _ptr(a), _ptr(b), int(side), _ptr(out))
+    return out
+
+
+def eigen_basis(cfg, UL, UR, side):
+    d = make_desc(cfg)
+    a = np.ascontiguousarray(UL, dtype=np.float64)
+    b = np.ascontiguousarray(UR, dtype=np.float64)
+    L = np.empty(25)
+    R = np.empty(25)
+    lam = np.empty(5)
+    lib().or_eigen_basis(ctypes.byref(d), _ptr(a), _ptr(b), int(side), _ptr(L), _ptr(R), _ptr(lam))
+    return L.reshape(5, 5), R.reshape(5, 5), lam
+
+
+def limiter(name_or_index, r):
+    idx = LIMITERS.index(name_or_index) if isinstance(name_or_index, str) else int(name_or_index)
+    return lib().or_limiter(idx, float(r))
+
+
+def num_threads():
+    return int(lib().or_num_threads())

@@ -1,0 +1,79 @@
+"""The C-ABI library on a machine without a GPU: it builds, loads, exports
+every entry point include/hydrocuda.h declares, and rejects bad arguments
+before touching the device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "hydrocuda.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(hc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_and_binding_agree():
+    import hydrocuda
+    names = declared_functions()
+    assert len(names) >= 30
+    assert sorted(hydrocuda.PROTOTYPES) == names
+
+
+def test_library_exports_every_declared_symbol():
+    import hydrocuda
+    L = hydrocuda.load_library()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+    assert L.hc_version().decode() == "0.3"
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """ctypes mirrors of the ABI structs have the C compiler's sizes and field offsets."""
+    import subprocess
+    import hydrocuda
+    structs = {"hc_solver_desc": hydrocuda.SolverDesc, "hc_batch_desc": hydrocuda.BatchDesc,
+               "hc_done": hydrocuda.Done, "hc_batch_stats": hydrocuda.BatchStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hydrocuda.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%%s %%zu\\n", "%s", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%%s.%%s %%zu\\n", "%s", "%s", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = dict(l.split() for l in subprocess.check_output([str(exe)]).decode().splitlines())
+    for cname, py in structs.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got["%s.%s" % (cname, f)]) == getattr(py, f).offset, (cname, f)
+
+
+def test_bad_arguments_fail_before_the_device():
+    import hydrocuda
+    L = hydrocuda.load_library()
+    out = ctypes.c_void_p()
+    d = hydrocuda.make_desc(dict(dim=2, gridSize=[8, 8]))
+    assert L.hc_solver_create(None, ctypes.byref(d), ctypes.byref(out)) == -1
+    assert L.hc_solver_status(None) == -1
+    assert L.hc_batch_step(None, 1, None) == -1
+    assert b"NULL" in L.hc_last_error()
+
+
+def test_descriptor_mapping_follows_reference_names():
+    import hydrocuda
+    d = hydrocuda.make_desc(dict(dim=3, gridSize=[4, 5, 6], boundary={"xmin": "mirror", "zmax": "periodic"},
+                                 fluxLimiter="superbee", usePLM=None, integrator="Runge-Kutta 3, TVD",
+                                 eqnArgs={"heatCapacityRatio": 5 / 3}))
+    assert list(d.n) == [4, 5, 6]
+    assert list(d.boundary) == [2, 3, 3, 3, 3, 1]
+    assert d.flux_limiter == 18 and d.integrator == 9 and abs(d.gamma - 5 / 3) < 1e-15
+    with pytest.raises(ValueError):
+        hydrocuda.make_desc(dict(dim=1, gridSize=8, fluxLimiter="no such limiter"))
+    with pytest.raises(ValueError):
+        hydrocuda.make_desc(dict(dim=1, gridSize=8, flux="hll"))

@@ -1,0 +1,186 @@
+"""Batched and served solves: each result equals the same solve run alone,
+admission respects the HBM budget and the slot table, failures are contained
+to their own instance."""
+import numpy as np
+import pytest
+
+import cases
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def quad(hc, n, seed, **kw):
+    args = cases.c4_quadrant(n, **kw)
+    return args, hc.quadrant_state(args, hc.random_quadrants(hc.SplitMix64(seed)))
+
+
+SCHEME = dict(usePLM="plm cons", slopeLimiter="van Leer", integrator="Runge-Kutta 2")
+
+
+def alone(hc, ctx, args, cons, t_end, precision):
+    s = hc.Solver(ctx, precision=precision, **args)
+    s.resetState(cons)
+    n = s.run_until(t_end)
+    return s.getState(), n, s.t
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_each_result_same_alone_and_in_the_mix(hc, ctx, precision):
+    """Instances of different sizes, admitted at different times, give bit-identical
+    results to the same solves run one at a time."""
+    specs = [(37, 1, .05), (64, 2, .08), (100, 3, .03), (48, 4, .06), (130, 5, .04)]
+    probs = [quad(hc, n, seed) + (t_end,) for n, seed, t_end in specs]
+    b = hc.Batch(ctx, precision=precision, max_slots=8, **SCHEME)
+    slots = {}
+    for k, (args, cons, t_end) in enumerate(probs[:3]):
+        slots[k] = b.admit(args, cons, t_end, tag=k)
+    b.step(3)                      # the first three are already on the GPU ...
+    for k, (args, cons, t_end) in enumerate(probs[3:], start=3):
+        slots[k] = b.admit(args, cons, t_end, tag=k)   # ... when these arrive
+    results = {}
+    for _ in range(10000):
+        b.step(4)
+        for ev in b.poll():
+            results[ev["tag"]] = (b.fetch(ev["slot"]), ev["steps"], ev["t"], ev["status"])
+            b.retire(ev["slot"])
+        if len(results) == len(probs):
+            break
+    assert len(results) == len(probs)
+    for k, (args, cons, t_end) in enumerate(probs):
+        ref, n, t = alone(hc, ctx, args, cons, t_end, precision)
+        got, steps, tt, status = results[k]
+        assert status == 0
+        assert steps == n and tt == t
+        np.testing.assert_array_equal(got, ref)
+
+
+def test_fp64_batch_matches_oracle(hc, ctx):
+    b = hc.Batch(ctx, precision="f64", max_slots=4, **SCHEME)
+    probs = [quad(hc, n, seed) for n, seed in ((24, 11), (33, 12))]
+    for k, (args, cons) in enumerate(probs):
+        b.admit(args, cons, t_end=.05, tag=k)
+    got = {}
+    while len(got) < len(probs):
+        b.step(8)
+        for ev in b.poll():
+            got[ev["tag"]] = (b.fetch(ev["slot"]), ev["t"])
+    for k, (args, cons) in enumerate(probs):
+        orc = oracle.OracleSolver(args)
+        orc.reset_state(cons)
+        orc.run_until(.05)
+        assert got[k][1] == orc.t
+        np.testing.assert_array_equal(got[k][0][:, :5], orc.get_interior()[:, :5])
+
+
+def test_mixed_dimensions_in_one_batch(hc, ctx):
+    scheme = dict(usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2")
+    base = dict(mins=[-1, -1, -1], maxs=[1, 1, 1], boundary="freeflow", cfl=.3, **scheme)
+    probs = []
+    a1 = dict(base, dim=1, gridSize=[300])
+    probs.append((a1, hc.sod_state(a1), .05))
+    a2 = dict(base, dim=2, gridSize=[70, 50])
+    probs.append((a2, hc.quadrant_state(a2, hc.random_quadrants(hc.SplitMix64(3))), .04))
+    a3 = dict(base, dim=3, gridSize=[20, 18, 16])
+    probs.append((a3, hc.blast_state(a3), .03))
+    b = hc.Batch(ctx, precision="f32", max_slots=4, **scheme)
+    for k, (args, cons, t_end) in enumerate(probs):
+        b.admit(args, cons, t_end, tag=k)
+    got = {}
+    while len(got) < 3:
+        b.step(4)
+        for ev in b.poll():
+            got[ev["tag"]] = b.fetch(ev["slot"])
+    for k, (args, cons, t_end) in enumerate(probs):
+        ref, _, _ = alone(hc, ctx, args, cons, t_end, "f32")
+        np.testing.assert_array_equal(got[k], ref)
+
+
+def test_budget_and_slot_admission(hc, ctx):
+    args, cons = quad(hc, 64, 1)
+    probe = hc.Batch(ctx, precision="f32", max_slots=4, **SCHEME)
+    s = probe.admit(args, cons, 1.0)
+    one = probe.stats()["bytes_in_use"]
+    probe.retire(s)
+    assert probe.stats()["bytes_in_use"] == 0
+    # budget for two instances: the third is refused, then fits after a retire
+    b = hc.Batch(ctx, precision="f32", max_slots=8, hbm_budget=2 * one + one // 2, **SCHEME)
+    s0 = b.admit(args, cons, 1.0, tag=0)
+    b.admit(args, cons, 1.0, tag=1)
+    with pytest.raises(hc.HydroCudaError) as e:
+        b.admit(args, cons, 1.0, tag=2)
+    assert e.value.code == -4
+    assert b.try_admit(args, cons, 1.0, tag=2) is None
+    b.retire(s0)
+    assert b.try_admit(args, cons, 1.0, tag=2) is not None
+    # slot table
+    c = hc.Batch(ctx, precision="f32", max_slots=1, **SCHEME)
+    c.admit(args, cons, 1.0)
+    with pytest.raises(hc.HydroCudaError) as e:
+        c.admit(args, cons, 1.0)
+    assert e.value.code == -5
+
+
+def test_nonfinite_request_is_contained(hc, ctx):
+    """A request whose host state holds a NaN finishes with HC_ERR_NONFINITE;
+    the others in the batch finish normally and match their alone runs."""
+    b = hc.Batch(ctx, precision="f32", max_slots=4, **SCHEME)
+    good_args, good = quad(hc, 40, 8)
+    bad_args, bad = quad(hc, 40, 9)
+    bad = bad.copy()
+    bad[123, 4] = np.nan
+    b.admit(good_args, good, .04, tag=0)
+    b.admit(bad_args, bad, .04, tag=1)
+    events = {}
+    while len(events) < 2:
+        b.step(4)
+        for ev in b.poll():
+            events[ev["tag"]] = ev
+            if ev["tag"] == 0:
+                events["state"] = b.fetch(ev["slot"])
+    assert events[1]["status"] == -6
+    assert events[0]["status"] == 0
+    ref, _, _ = alone(hc, ctx, good_args, good, .04, "f32")
+    np.testing.assert_array_equal(events["state"], ref)
+
+
+def test_autotune_keeps_results(hc, ctx, tmp_path):
+    """Tile shape changes the schedule, not the arithmetic: results stay bit-identical."""
+    probs = [quad(hc, n, s) for n, s in ((150, 21), (90, 22))]
+    outs = []
+    for tune in (False, True):
+        b = hc.Batch(ctx, precision="f32", max_slots=4, **SCHEME)
+        for k, (args, cons) in enumerate(probs):
+            b.admit(args, cons, .03, tag=k)
+        if tune:
+            cache = str(tmp_path / "tune.txt")
+            b.autotune(cache)
+            assert open(cache).read().strip()
+            b.autotune(cache)      # second call reads the cache
+        got = {}
+        while len(got) < 2:
+            b.step(4)
+            for ev in b.poll():
+                got[ev["tag"]] = b.fetch(ev["slot"])
+        outs.append(got)
+    for k in range(2):
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])
+
+
+def test_served_stream_results_match_alone(hc, ctx):
+    """A small Poisson stream through the serving loop: every result equals its alone run."""
+    import serve
+    reqs = serve.synthetic_stream(12, rate_hz=400.0, seed=5, scale=0.08)
+    inputs = {r.tag: (r.args, r.cons.copy(), r.t_end) for r in reqs}
+    b = hc.Batch(ctx, precision="f32", max_slots=6, hbm_budget=1 << 30,
+                 usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2")
+    srv = serve.Server(b, steps_per_tick=4)
+    done = srv.run(reqs)
+    assert len(done) == len(reqs)
+    lat = serve.latency_summary(done)
+    assert lat["p99_s"] >= lat["p50_s"] > 0
+    for r in done:
+        args, cons, t_end = inputs[r.tag]
+        ref, n, t = alone(hc, ctx, args, cons, t_end, "f32")
+        assert r.status == 0 and r.steps == n
+        np.testing.assert_array_equal(r.result, ref)

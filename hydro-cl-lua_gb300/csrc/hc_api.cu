@@ -40,6 +40,7 @@ struct hc_solver {
     FusedSet* fused = nullptr;
     double t = 0;           // plain form: SolverBase.t (a Lua double in the reference)
     long long steps = 0;
+    int plain_status = HC_OK;   // plain form: first non-finite dt seen
 };
 
 struct hc_batch {
@@ -162,7 +163,7 @@ int hc_solver_create(hc_context* ctx, const hc_solver_desc* desc, hc_solver** ou
         r = plain_create(*desc, ctx->stream, &s->plain);
     } else {
         r = fused_create(scheme_of(*desc), 1, ctx->stream, &s->fused);
-        if (r == HC_OK) r = fused_add(s->fused, 0, *desc, nullptr, HC_LAYOUT_AOS6_F64, INFINITY, LLONG_MAX);
+        if (r == HC_OK) r = fused_add(s->fused, 0, *desc, nullptr, HC_LAYOUT_AOS6_F64, INFINITY, LLONG_MAX, 0);
     }
     if (r != HC_OK) {
         std::string const msg = g_last_error;
@@ -197,7 +198,6 @@ int hc_solver_reset_state(hc_solver* s, const void* cons, int layout) {
         return HC_OK;
     }
     HC_CHECK(fused_set_state(s->fused, 0, cons, layout, 1));
-    HC_CHECK(fused_set_time(s->fused, 0, 0.));
     return fused_sync(s->fused);
 }
 
@@ -265,7 +265,7 @@ int hc_solver_step(hc_solver* s, double dt) {
 }
 
 static int solver_status(hc_solver* s) {
-    if (s->plain) return HC_OK;
+    if (s->plain) return s->plain_status == HC_OK ? HC_OK : fail(s->plain_status, "calcDT produced a non-finite dt");
     std::vector<SlotInfo> info;
     HC_CHECK(fused_slot_info(s->fused, info));
     if (info[0].status & DEV_TIMEOUT) return fail(HC_ERR_TIMEOUT, "a bounded device wait ran out");
@@ -279,7 +279,8 @@ int hc_solver_update(hc_solver* s, double* dt_out) {
     if (s->plain) {
         double dt;
         HC_CHECK(plain_calc_dt(s->plain, s->d.cfl, s->d.fixed_dt, &dt));
-        if (!std::isfinite(dt)) return fail(HC_ERR_NONFINITE, "calcDT produced a non-finite dt");
+        // the reference prints "got a bad dt" and steps on (solverbase.lua:3017-3019)
+        if (!std::isfinite(dt)) s->plain_status = HC_ERR_NONFINITE;
         HC_CHECK(plain_step(s->plain, s->d.integrator, dt));
         s->t = s->t + dt;
         s->steps += 1;
@@ -295,7 +296,7 @@ int hc_solver_update(hc_solver* s, double* dt_out) {
     HC_CHECK(fused_sync(s->fused));
     HC_CHECK(fused_slot_info(s->fused, info));
     if (dt_out) *dt_out = info[0].dt;
-    return solver_status(s);
+    return HC_OK;
 }
 
 int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long long* steps_done) {
@@ -307,9 +308,10 @@ int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long lo
         while (!(s->t >= t_end) && n < max_steps) {
             HC_CHECK(hc_solver_update(s, nullptr));
             ++n;
+            if (!std::isfinite(s->t)) break;   // t can no longer reach t_end
         }
         if (steps_done) *steps_done = n;
-        return HC_OK;
+        return std::isfinite(s->t) ? HC_OK : fail(HC_ERR_NONFINITE, "time became non-finite");
     }
     std::vector<SlotInfo> info;
     HC_CHECK(fused_slot_info(s->fused, info));
@@ -325,7 +327,7 @@ int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long lo
         if (chunk < 64) chunk *= 2;
     }
     if (steps_done) *steps_done = info[0].steps - start;
-    return solver_status(s);
+    return std::isfinite(info[0].t) ? HC_OK : fail(HC_ERR_NONFINITE, "time became non-finite");
 }
 
 int hc_solver_get_time(hc_solver* s, double* t) {
@@ -410,7 +412,7 @@ int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, in
     for (int k = 0; k < b->d.max_slots; ++k)
         if (!b->used[k]) { s = k; break; }
     if (s < 0) return fail(HC_ERR_NO_SLOT, "every slot is in use");
-    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps));
+    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps, 1));
     b->used[s] = 1;
     b->reported[s] = 0;
     b->tags[s] = tag;
@@ -433,6 +435,13 @@ int hc_batch_step(hc_batch* b, int steps, int* n_active) {
         *n_active = n;
     }
     return HC_OK;
+}
+
+int hc_batch_step_timed(hc_batch* b, int steps, double* stage_ms, int n_stage_ms, double* total_ms) {
+    if (!b || !total_ms || (n_stage_ms > 0 && !stage_ms)) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(b->ctx));
+    HC_CHECK(fused_steps_timed(b->fused, steps, stage_ms, n_stage_ms, total_ms));
+    return fused_sync(b->fused);
 }
 
 int hc_batch_poll(hc_batch* b, hc_done* out, int cap, int* n_out) {

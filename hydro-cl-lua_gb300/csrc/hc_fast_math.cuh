@@ -69,6 +69,7 @@ __device__ __forceinline__ T limiter(int which, T r) {
     case 17: return tmax(z, tmin(two, tmin(T(.5) * (one + r), two * r)));
     case 18: return tmax(z, tmax(tmin(one, two * r), tmin(two, r)));
     case 19: return T(.5) * (r + one) * tmin(one, tmin(M<T>::div(T(4) * r, r + one), M<T>::div(T(4), r + one)));
+    case 20: return M<T>::div(r + fabs(r), one + fabs(r));
     }
     return z;
 }

@@ -58,6 +58,7 @@ struct DevInst {
     int zeroFlux[3];       // area <= 1e-7: calcFlux writes a zero flux
     double gamma, rhoMin, PMin, cfl, fixed_dt, t_end;
     long long max_steps;
+    int stop_on_error;     // 1 (batched solves): a non-finite state or dt ends the instance
     void* buf[kMaxBufs];
     void* dbuf[kMaxDBufs];
 };

@@ -44,11 +44,15 @@ __global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin,
     c.dtmin[c.par ^ 1] = kInfBits;
     if (!c.active) return;
     const DevInst& I = inst[s];
-    if (c.status != 0) { c.active = 0; c.done = 1; return; }
+    if (c.status != 0 && I.stop_on_error) { c.active = 0; c.done = 1; return; }
     // app.lua:1590: the exit test precedes the update
     if (c.t >= I.t_end || c.steps >= I.max_steps) { c.active = 0; c.done = 1; return; }
     double const dt = I.fixed_dt > 0 ? I.fixed_dt : I.cfl * __longlong_as_double((long long)c.dtmin[c.par]);
-    if (!(dt > 0) || !isfinite(dt)) { c.status = DEV_NONFINITE; c.active = 0; c.done = 1; return; }
+    if (!(dt > 0) || !isfinite(dt)) {
+        // the reference reports a bad dt and steps on with it (solverbase.lua:3017-3019)
+        c.status |= DEV_NONFINITE;
+        if (I.stop_on_error || !(dt == dt)) { c.active = 0; c.done = 1; return; }
+    }
     c.dt = dt;
     c.stepping = 1;
 }
@@ -83,6 +87,19 @@ __global__ void k_tune_mode(DevCtl* ctl, const DevInst* inst, int nslots, int on
 
 __global__ void k_reset_dtmin(DevCtl* ctl, int slot) {
     ctl[slot].dtmin[ctl[slot].par] = kInfBits;
+}
+
+// A fresh state (resetState): clear time, step count and status; the dt
+// parity and the buffer rotation stay, since they locate the state.
+__global__ void k_restart(DevCtl* ctl, int slot) {
+    DevCtl& c = ctl[slot];
+    c.t = 0.;
+    c.dt = 0.;
+    c.steps = 0;
+    c.status = 0;
+    c.done = 0;
+    c.active = 1;
+    c.stepping = 0;
 }
 
 }  // namespace fz
@@ -364,6 +381,7 @@ int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int res
     HC_CHECK(ensure_staging(f, bytes));
     HC_CUDA(cudaMemcpyAsync(f->staging, host, bytes, cudaMemcpyHostToDevice, f->stream));
     int const b = state_buf(f, slot);
+    if (reset) fz::k_restart<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
     A->xfer(f->d_inst, slot, b, f->staging, layout, 0, f->stream);
     if (reset) A->constrain(f->d_inst, slot, b, f->stream);
     A->fill_ghosts(f->d_inst, slot, b, f->stream);
@@ -387,7 +405,8 @@ int fused_get_state(FusedSet* f, int slot, void* host, int layout) {
     return HC_OK;
 }
 
-int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout, double t_end, long long max_steps) {
+int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout, double t_end, long long max_steps,
+              int stop_on_error) {
     if (slot < 0 || slot >= f->max_slots || f->slots[slot].used) return fail(HC_ERR_STATE, "slot unavailable");
     HC_CHECK(validate(f, d));
     Slot& S = f->slots[slot];
@@ -438,6 +457,7 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     I.fixed_dt = d.fixed_dt;
     I.t_end = t_end;
     I.max_steps = max_steps;
+    I.stop_on_error = stop_on_error;
     char* p = (char*)S.mem;
     for (int b = 0; b < nb; ++b, p += planeBytes * 5) I.buf[b] = p;
     for (int b = 0; b < nd; ++b, p += planeBytes * 5) I.dbuf[b] = p;
@@ -584,6 +604,45 @@ int fused_steps(FusedSet* f, int steps) {
     return HC_OK;
 }
 
+int fused_steps_timed(FusedSet* f, int steps, double* stage_ms, int n_stage_ms, double* total_ms) {
+    if (steps <= 0) return HC_OK;
+    HC_CHECK(rebuild_items(f));
+    if (!f->graph_dims_mask) return HC_OK;
+    const IntegratorPlan& P = f->plan[0];
+    std::vector<cudaEvent_t> ev((size_t)steps * P.n_stages * 2 + 2);
+    for (auto& e : ev) HC_CUDA(cudaEventCreate(&e));
+    size_t k = 0;
+    HC_CUDA(cudaEventRecord(ev[k++], f->stream));
+    unsigned const g = (unsigned)((f->max_slots + 127) / 128);
+    for (int s = 0; s < steps; ++s) {
+        fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates);
+        for (int st = 0; st < P.n_stages; ++st) {
+            IntegratorPlan one;
+            std::memset(&one, 0, sizeof(one));
+            one.n_stages = 1;
+            one.stage[0] = P.stage[st];
+            HC_CUDA(cudaEventRecord(ev[k++], f->stream));
+            HC_CHECK(launch_stages(f, one, f->graph_dims_mask));
+            HC_CUDA(cudaEventRecord(ev[k++], f->stream));
+        }
+    }
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates);
+    HC_CUDA(cudaEventRecord(ev[k++], f->stream));
+    HC_CUDA(cudaEventSynchronize(ev[k - 1]));
+    size_t j = 1;
+    for (int s = 0; s < steps; ++s)
+        for (int st = 0; st < P.n_stages; ++st, j += 2) {
+            float ms = 0;
+            HC_CUDA(cudaEventElapsedTime(&ms, ev[j], ev[j + 1]));
+            if (st < n_stage_ms) stage_ms[st] += ms;
+        }
+    float tot = 0;
+    HC_CUDA(cudaEventElapsedTime(&tot, ev[0], ev[k - 1]));
+    *total_ms += tot;
+    for (auto& e : ev) cudaEventDestroy(e);
+    return HC_OK;
+}
+
 int fused_step_dt(FusedSet* f, int slot, double dt) {
     HC_CHECK(rebuild_items(f));
     const Slot& S = f->slots[slot];
@@ -702,6 +761,12 @@ int fused_stats(FusedSet* f, hc_batch_stats* st) {
         if (info[s].active) { st->active++; st->cells += f->slots[s].cells; }
     }
     st->tiles = (long long)f->h_nitems[0] + f->h_nitems[1] + f->h_nitems[2];
+    st->n_stages = f->plan[0].n_stages;
+    for (int d = 0; d < 3; ++d) {
+        st->tile[d][0] = f->launcher[d] ? f->launcher[d]->tx : 0;
+        st->tile[d][1] = f->launcher[d] ? f->launcher[d]->ty : 0;
+        st->tile[d][2] = f->launcher[d] ? f->launcher[d]->tz : 0;
+    }
     return HC_OK;
 }
 

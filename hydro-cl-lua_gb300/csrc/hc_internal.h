@@ -116,13 +116,16 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
 void fused_destroy(FusedSet* f);
 // bytes an instance of this shape holds on the device
 size_t fused_instance_bytes(const FusedSet* f, const hc_solver_desc& d);
+// stop_on_error: a non-finite state or dt ends the instance (batches); the
+// single-solver form steps on like the reference and only records the status.
 int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout,
-              double t_end, long long max_steps);
+              double t_end, long long max_steps, int stop_on_error);
 int fused_remove(FusedSet* f, int slot);
 int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int reset);
 int fused_get_state(FusedSet* f, int slot, void* host, int layout);
 // Runs `steps` updates of every live instance (device-side completion tests).
 int fused_steps(FusedSet* f, int steps);
+int fused_steps_timed(FusedSet* f, int steps, double* stage_ms, int n_stage_ms, double* total_ms);
 // One update of the given slot's instance with an explicit dt (-1: CFL dt).
 int fused_step_dt(FusedSet* f, int slot, double dt);
 int fused_calc_dt(FusedSet* f, int slot, double* dt);

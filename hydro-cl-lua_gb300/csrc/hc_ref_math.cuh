@@ -50,6 +50,7 @@ __device__ __forceinline__ double limiter(int which, double r) {
     case 17: return clmax(0., clmin(2., clmin(.5 * (1. + r), 2. * r)));             // monotized central
     case 18: return clmax(0., clmax(clmin(1., 2. * r), clmin(2., r)));             // superbee
     case 19: return .5 * (r + 1.) * clmin(1., clmin(4. * r / (r + 1.), 4. / (r + 1.))); // Barth-Jespersen
+    case 20: return (r + fabs(r)) / (1. + fabs(r));                                 // van Leer, app.lua:631 comment
     }
     return 0.;
 }

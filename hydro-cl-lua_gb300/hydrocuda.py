@@ -30,6 +30,10 @@ LIMITERS = [
     "HQUICK", "Koren", "minmod", "Oshker", "ospre", "smart", "Sweby", "UMIST",
     "van Albada 1", "van Albada 2", "van Leer", "monotized central",
     "superbee", "Barth-Jespersen",
+    # beyond the reference's table: the van Leer form the reference keeps in a
+    # comment (hydro/app.lua:631), equal to "van Leer" except at r = -1, where
+    # the table's expression is 0/0
+    "van Leer (abs)",
 ]
 # hydro/int/all.lua (explicit integrators)
 INTEGRATORS = [
@@ -81,7 +85,8 @@ class Done(ctypes.Structure):
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("active", ctypes.c_int), ("occupied", ctypes.c_int), ("bytes_in_use", ctypes.c_size_t),
-                ("tiles", ctypes.c_longlong), ("cells", ctypes.c_longlong)]
+                ("tiles", ctypes.c_longlong), ("cells", ctypes.c_longlong), ("n_stages", ctypes.c_int),
+                ("tile", (ctypes.c_int * 3) * 3)]
 
 
 # every entry point of include/hydrocuda.h with its argument types
@@ -114,6 +119,7 @@ PROTOTYPES = {
     "hc_batch_admit": (_ip, [_vp, ctypes.POINTER(SolverDesc), _vp, _ip, ctypes.c_double, ctypes.c_longlong,
                              ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_int)]),
     "hc_batch_step": (_ip, [_vp, _ip, ctypes.POINTER(ctypes.c_int)]),
+    "hc_batch_step_timed": (_ip, [_vp, _ip, _dp, _ip, _dp]),
     "hc_batch_poll": (_ip, [_vp, ctypes.POINTER(Done), _ip, ctypes.POINTER(ctypes.c_int)]),
     "hc_batch_fetch": (_ip, [_vp, _ip, _vp, _ip]),
     "hc_batch_retire": (_ip, [_vp, _ip]),
@@ -425,6 +431,14 @@ class Batch:
         _check(self.L.hc_batch_step(self.h, int(steps), ctypes.byref(n)))
         return n.value
 
+    def step_timed(self, steps=1):
+        """Steps with CUDA events around each stage kernel; returns (stage_ms list, total_ms)."""
+        n = self.stats()["n_stages"]
+        st = (ctypes.c_double * max(n, 1))()
+        tot = ctypes.c_double(0.0)
+        _check(self.L.hc_batch_step_timed(self.h, int(steps), st, n, ctypes.byref(tot)))
+        return [st[i] for i in range(n)], tot.value
+
     def poll(self, cap=4096):
         arr = (Done * cap)()
         n = ctypes.c_int()
@@ -451,7 +465,8 @@ class Batch:
     def stats(self):
         s = BatchStats()
         _check(self.L.hc_batch_stats_get(self.h, ctypes.byref(s)))
-        return dict(active=s.active, occupied=s.occupied, bytes_in_use=s.bytes_in_use, tiles=s.tiles, cells=s.cells)
+        return dict(active=s.active, occupied=s.occupied, bytes_in_use=s.bytes_in_use, tiles=s.tiles, cells=s.cells,
+                    n_stages=s.n_stages, tile=[list(s.tile[d]) for d in range(3)])
 
     def conservation(self, slot):
         s = (ctypes.c_double * 5)()

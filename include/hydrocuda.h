@@ -78,7 +78,12 @@ extern "C" {
 #define HC_LIMITER_MONOTIZED_CENTRAL 17
 #define HC_LIMITER_SUPERBEE         18
 #define HC_LIMITER_BARTH_JESPERSEN  19
-#define HC_NUM_LIMITERS             20
+/* Not a row of the reference's table: the van Leer form the reference keeps
+ * beside its table entry as a comment (hydro/app.lua:631),
+ * (r + |r|) / (1 + |r|).  It equals the table's max(0, r) * 2 / (1 + r) for
+ * every r except r = -1, where the table's expression divides 0 by 0. */
+#define HC_LIMITER_VAN_LEER_ABS     20
+#define HC_NUM_LIMITERS             21
 
 /* usePLM (hydro/solver/plm.cl) */
 #define HC_RECON_NONE                0   /* usePLM = nil: interface states are the cell states */
@@ -211,6 +216,8 @@ typedef struct hc_batch_stats {
     size_t    bytes_in_use;      /* device state bytes charged to the budget */
     long long tiles;             /* tiles in the current work list */
     long long cells;             /* interior cells of live instances */
+    int       n_stages;          /* stage launches per update and dimension */
+    int       tile[3][3];        /* tile shape (x, y, z) in use per dimension 1..3 */
 } hc_batch_stats;
 
 int hc_batch_create(hc_context* ctx, const hc_batch_desc* desc, hc_batch** out);
@@ -225,6 +232,12 @@ int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, in
 /* Advances every live instance by up to `steps` updates (each instance with its
  * own CFL dt), in batched launches.  *n_active = instances still stepping. */
 int hc_batch_step(hc_batch* b, int steps, int* n_active);
+/* Measurement form of hc_batch_step: the same launches, issued directly (not
+ * from the captured graph) with CUDA events around every stage kernel on the
+ * batch's stream.  Adds the elapsed milliseconds of stage s (all dimensions,
+ * summed over the steps) to stage_ms[s] for s < n_stage_ms, and of the whole
+ * span to *total_ms. */
+int hc_batch_step_timed(hc_batch* b, int steps, double* stage_ms, int n_stage_ms, double* total_ms);
 /* Lists finished instances not yet reported (at most cap). */
 int hc_batch_poll(hc_batch* b, hc_done* out, int cap, int* n_out);
 /* Copies a slot's interior state to the host. */

@@ -77,6 +77,8 @@ static real limiter(int which, real r) {
 	case 17: return cl_max(0., cl_min(2., cl_min(.5 * (1. + r), 2. * r)));    // monotized central
 	case 18: return cl_max(0., cl_max(cl_min(1., 2. * r), cl_min(2., r)));    // superbee
 	case 19: return .5 * (r + 1.) * cl_min(1., cl_min(4. * r / (r + 1.), 4. / (r + 1.))); // Barth-Jespersen
+	// Not in the table: the van Leer form kept as a comment at app.lua:631.
+	case 20: return (r + std::fabs(r)) / (1. + std::fabs(r));
 	}
 	return 0.;
 }

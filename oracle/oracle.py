@@ -28,6 +28,9 @@ LIMITERS = [
     "HQUICK", "Koren", "minmod", "Oshker", "ospre", "smart", "Sweby", "UMIST",
     "van Albada 1", "van Albada 2", "van Leer", "monotized central",
     "superbee", "Barth-Jespersen",
+    # not a row of the reference's table: the van Leer form of the comment at
+    # hydro/app.lua:631, (r + |r|) / (1 + |r|)
+    "van Leer (abs)",
 ]
 # Explicit integrators (hydro/int/all.lua), in the oracle's numbering.
 INTEGRATORS = [

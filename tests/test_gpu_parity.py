@@ -32,9 +32,14 @@ def initial_state(hc, args, kind):
 
 
 def rel_linf(a, b):
-    """max |a - b| over all cells and fields, relative to max |b| of the same field."""
-    scale = np.maximum(np.max(np.abs(b), axis=0), 1e-300)
-    return float(np.max(np.abs(a - b) / scale))
+    """max |a - b| over all cells and fields, relative to max |b| of the same field;
+    non-finite values must sit in the same places (they are then not compared)."""
+    fin = np.isfinite(a) & np.isfinite(b)
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    if not fin.any():
+        return 0.0
+    scale = np.maximum(np.max(np.where(fin, np.abs(b), 0), axis=0), 1e-300)
+    return float(np.max(np.where(fin, np.abs(a - b), 0) / scale))
 
 
 def l1_rho(a, b):
@@ -60,6 +65,8 @@ SMALL_CASES = [
     ("kh_64", cases.c2_kh(64), "kh", 6),
     ("blast_16", cases.c3_blast(16), "blast", 4),
     ("quadrant_40", cases.c4_quadrant(40), "quadrant", 6),
+    # the table's van Leer: non-finite after ~6 steps in the reference's own arithmetic
+    ("quadrant_40_vanleer_table", cases.c4_quadrant(40, slopeLimiter="van Leer"), "quadrant", 9),
     ("sod2d_mirror_vanleer_flux", dict(cases.c1_sod(dim=2, gridSize=[24, 20], boundary="mirror", fluxLimiter="van Leer")), "sod", 6),
     ("sod3d_periodic_rk4", dict(cases.c3_blast(10, boundary="periodic", integrator="Runge-Kutta 4", usePLM=None,
                                               slopeLimiter="donor cell")), "blast", 3),
@@ -82,6 +89,10 @@ def test_fp64_forms_match_oracle_per_step(hc, ctx, precision, name, args, kind, 
         assert rel_linf(g, o) <= REL_LINF_PER_STEP, (name, k)
         np.testing.assert_array_equal(g, o)
     assert abs(gpu.t - orc.t) == 0.0
+    if "table" in name:
+        assert not np.all(np.isfinite(o)), "expected the reference's van Leer to go non-finite"
+        if precision != "f64 plain":
+            assert gpu.status() == -6
 
 
 def test_plain_ghost_cells_match_oracle(hc, ctx):
@@ -133,7 +144,10 @@ def test_every_limiter(hc, ctx, limiter):
             assert np.array_equal(g, o, equal_nan=True)
 
 
-@pytest.mark.parametrize("name,args,kind,steps", SMALL_CASES, ids=[c[0] for c in SMALL_CASES])
+FINITE_CASES = [c for c in SMALL_CASES if "table" not in c[0]]
+
+
+@pytest.mark.parametrize("name,args,kind,steps", FINITE_CASES, ids=[c[0] for c in FINITE_CASES])
 def test_fp32_form_density_l1(hc, ctx, name, args, kind, steps):
     gpu, orc = make_pair(hc, ctx, args, kind, "f32")
     for _ in range(steps):

@@ -235,6 +235,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--count", type=int, default=COUNT,
+                    help="instances (the configuration has 512; fewer only for profiling a small case)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -253,7 +256,7 @@ def main():
 
     import hydrocuda as hc
     ctx = hc.Context(local)
-    work = workload(rank=rank)
+    work = workload(count=args.count, rank=rank)
     cells = sum(a["gridSize"][0] * a["gridSize"][1] for a, _ in work)
     inputs = [soa5_f32(hc, a, q) for a, q in work]
     b = hc.Batch(ctx, precision="f32", max_slots=len(work), **SCHEME)
@@ -306,7 +309,8 @@ def main():
     if rank == 0 and not args.no_e2e:
         out["e2e"] = e2e_run(hc, ctx, work, inputs, cells)
     if rank == 0:
-        out["fp64"] = fp64_run(hc, ctx, work)
+        if not args.no_fp64:
+            out["fp64"] = fp64_run(hc, ctx, work)
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(work)
         print(json.dumps(out))

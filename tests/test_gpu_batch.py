@@ -15,7 +15,7 @@ def quad(hc, n, seed, **kw):
     return args, hc.quadrant_state(args, hc.random_quadrants(hc.SplitMix64(seed)))
 
 
-SCHEME = dict(usePLM="plm cons", slopeLimiter="van Leer", integrator="Runge-Kutta 2")
+SCHEME = dict(usePLM="plm cons", slopeLimiter="van Leer (abs)", integrator="Runge-Kutta 2")
 
 
 def alone(hc, ctx, args, cons, t_end, precision):

@@ -227,6 +227,26 @@ __device__ __forceinline__ void roe(T* F, const Eos<T>& s, const C5<T>& UL, cons
     right(F, C.e, fe);
 }
 
+// Roe flux without the flux limiter, from the two one-sided projections:
+// with sgn(lambda) lambda = |lambda|, the reference's
+//   lambda L.(UL+UR)/2 - |lambda| L.(UR-UL)/2
+// equals max(lambda, 0) L.UL + min(lambda, 0) L.UR component by component.
+template <typename T>
+__device__ __forceinline__ void roeSplit(T* F, const Eos<T>& s, const C5<T>& UL, const C5<T>& UR) {
+    EigF<T> e;
+    eigen(e, s, UL, UR);
+    T wL[5], wR[5], fe[5];
+    left(wL, e, s, UL.u);
+    left(wR, e, s, UR.u);
+    T const lam[3] = {e.vn - e.Cs, e.vn, e.vn + e.Cs};
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        T const l = lam[j == 0 ? 0 : (j == 4 ? 2 : 1)];
+        fe[j] = fmaxf(l, T(0)) * wL[j] + fminf(l, T(0)) * wR[j];
+    }
+    right(F, e, fe);
+}
+
 // "plm cons" slope of one component: returns sigma.
 template <typename T>
 __device__ __forceinline__ T plmSigma(T um, T u0, T up, int lim) {

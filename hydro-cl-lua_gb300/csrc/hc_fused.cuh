@@ -295,10 +295,12 @@ struct BoxGeom {
 // Sweeps one segment of L cells along AXIS.  `base` is the box index of the
 // segment's first cell.  emit(k, FL, FR) receives, for cell k of the segment,
 // its left and right face fluxes in the global frame (5 components).
-template <typename T, int AXIS, int STRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, class Emit>
-__device__ __forceinline__ void sweepSegment(const T* box, int base, const DevInst& I, int slopeLim, int fluxLim,
+template <typename T, int AXIS, int STRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, int SLOPE, class Emit>
+__device__ __forceinline__ void sweepSegment(const T* box, int base, const DevInst& I, int slopeLimRT, int fluxLim,
                                              double dt, Emit&& emit) {
-    if (EXACT) {
+    // SLOPE >= 0 fixes the slope limiter at compile time; -1 dispatches on slopeLimRT
+    int const slopeLim = SLOPE >= 0 ? SLOPE : slopeLimRT;
+    if constexpr (EXACT) {
         ref::Eos const e = refEos<T>(I, slopeLim, fluxLim);
         double const dt_dx = dt / I.grid_dx[AXIS];
         auto load = [&](int k, double* U) {
@@ -313,7 +315,7 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const DevIn
             if (zero) { for (int j = 0; j < 6; ++j) out[j] = 0.; return; }
             ref::roeFlux(out, e, UL, UR, C, IL, IR, AXIS, LIM, dt_dx);
         };
-        if (PLM) {
+        if constexpr (PLM) {
             double Um[6], U0[6], Up[6], prevR[6], fL[6], fR[6];
             load(-2, Um);
             load(-1, U0);
@@ -329,7 +331,7 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const DevIn
                 }
                 for (int j = 0; j < 6; ++j) { prevR[j] = fR[j]; Um[j] = U0[j]; U0[j] = Up[j]; }
             }
-        } else if (LIM) {
+        } else if constexpr (LIM) {
             double Ua[6], Ub[6], Uc[6], Ud[6];
             ref::Iface IL, IC, IR;
             load(-2, Ua);
@@ -386,11 +388,11 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const DevIn
             out[A3] = Fr[3];
             out[4] = Fr[4];
         };
-        if (PLM) {
+        if constexpr (PLM) {
             C5 Um, U0, Up, prevR, fL, fR;
             load(-2, Um);
             load(-1, U0);
-#pragma unroll 1
+#pragma unroll
             for (int k = -1; k <= L; ++k) {
                 load(k + 1, Up);
 #pragma unroll
@@ -400,9 +402,14 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const DevIn
                     fR.u[j] = U0.u[j] + sg;
                 }
                 if (k >= 0) {
-                    fast::IfaceF<T> C;
-                    fast::makeIface(C, e, prevR, fL);
-                    flux(F, prevR, fL, C, C, C);
+                    T Fr[5];
+                    fast::roeSplit<T>(Fr, e, prevR, fL);
+                    if (zero) for (int j = 0; j < 5; ++j) Fr[j] = T(0);
+                    F[0] = Fr[0];
+                    F[A1] = Fr[1];
+                    F[A2] = Fr[2];
+                    F[A3] = Fr[3];
+                    F[4] = Fr[4];
                     if (k >= 1) emit(k - 1, Fprev, F);
 #pragma unroll
                     for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
@@ -411,7 +418,7 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const DevIn
                 Um = U0;
                 U0 = Up;
             }
-        } else if (LIM) {
+        } else if constexpr (LIM) {
             C5 Ua, Ub, Uc, Ud;
             fast::IfaceF<T> IL, IC, IR;
             load(-2, Ua);
@@ -435,12 +442,17 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const DevIn
         } else {
             C5 Ua, Ub;
             load(-1, Ua);
-#pragma unroll 1
+#pragma unroll
             for (int k = 0; k <= L; ++k) {
                 load(k, Ub);
-                fast::IfaceF<T> C;
-                fast::makeIface(C, e, Ua, Ub);
-                flux(F, Ua, Ub, C, C, C);
+                T Fr[5];
+                fast::roeSplit<T>(Fr, e, Ua, Ub);
+                if (zero) for (int j = 0; j < 5; ++j) Fr[j] = T(0);
+                F[0] = Fr[0];
+                F[A1] = Fr[1];
+                F[A2] = Fr[2];
+                F[A3] = Fr[3];
+                F[4] = Fr[4];
                 if (k >= 1) emit(k - 1, Fprev, F);
 #pragma unroll
                 for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
@@ -467,7 +479,7 @@ struct StageCfg {
 
 constexpr unsigned kSpinLimit = 1u << 22;
 
-template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM>
+template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM, int SLOPE>
 __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs a, int slopeLim, int fluxLim) {
     using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
     using G = typename Cfg::G;
@@ -516,7 +528,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
         int const nx = I.n[0], ny = I.n[1], nz = I.n[2];
 
         // ---- all axes but the last: flux differences into D ----------------
-        if (DIM >= 2) {
+        if constexpr (DIM >= 2) {
 #pragma unroll 1
             for (int axis = 0; axis < DIM - 1; ++axis) {
                 if (axis == 0) {
@@ -531,7 +543,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                         if (x0 + cx0 >= nx || y0 + cy >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + (DIM > 2 ? 2 : 0)) * G::BY + (cy + 2)) * G::BX + (cx0 + 2);
                         T* Dl = D + (cz * TY + cy) * G::DPX + cx0;
-                        sweepSegment<T, 0, 1, G::BOXN, L, EXACT, PLM, LIM>(box, base, I, slopeLim, fluxLim, dt,
+                        sweepSegment<T, 0, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, I, slopeLim, fluxLim, dt,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                                 for (int f = 0; f < 5; ++f) {
@@ -541,8 +553,8 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                                 }
                             });
                     }
-                } else {
-                    // axis 1 of a 3D tile (only reached when DIM == 3)
+                } else if constexpr (DIM == 3) {
+                    // axis 1 of a 3D tile
                     constexpr int nlines = TX * TZ;
                     constexpr int nseg = TY / L;
                     double const ar = I.area[1];
@@ -554,7 +566,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                         if (x0 + cx >= nx || y0 + cy0 >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + 2) * G::BY + (cy0 + 2)) * G::BX + (cx + 2);
                         T* Dl = D + (cz * TY + cy0) * G::DPX + cx;
-                        sweepSegment<T, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM>(box, base, I, slopeLim, fluxLim, dt,
+                        sweepSegment<T, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, I, slopeLim, fluxLim, dt,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                                 for (int f = 0; f < 5; ++f) {
@@ -600,7 +612,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             if (gx0 >= nx || gy0 >= ny || gz0 >= nz) continue;
             int const base = ((c0[2] + (DIM > 2 ? 2 : 0)) * G::BY + (c0[1] + (DIM > 1 ? 2 : 0))) * G::BX + (c0[0] + 2);
             int const dbase = (c0[2] * TY + c0[1]) * G::DPX + c0[0];
-            sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM>(box, base, I, slopeLim, fluxLim, dt,
+            sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, I, slopeLim, fluxLim, dt,
                 [&](int k, const auto* FL, const auto* FR) {
                     int g[3] = {gx0, gy0, gz0};
                     g[AX] += k;
@@ -640,7 +652,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
 #pragma unroll
                     for (int f = 0; f < 5; ++f) {
                         out[f * I.plane + idx] = u[f];
-                        bad |= !isfinite((double)u[f]);
+                        bad |= !isfinite(u[f]);
                     }
                     scatterGhosts<T, DIM>(I, out, g[0], g[1], g[2], u);
                     if (dstore) {
@@ -791,6 +803,7 @@ struct StageLauncher {
     int precision;   // HC_F32_FUSED / HC_F64_FUSED
     int dim;
     bool plm, lim;
+    int slope;       // slope limiter compiled in, or -1 (any, dispatched at run time)
     int variant;     // tile-shape candidate index
     int tx, ty, tz, nthreads;
     size_t smem;

@@ -9,8 +9,8 @@ void register_f32_d3(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& a
     constexpr int P = HC_F32_FUSED;
     constexpr bool E = false;
     // variants: 32x8x8 (256 thr), 16x8x8 (128 thr); L = 8
-    add_stage<T, P, 3, 0, 32, 8, 8, 8, 256, E, true, false>(st);
-    add_stage<T, P, 3, 1, 16, 8, 8, 8, 128, E, true, false>(st);
+    add_plm_set<T, P, 3, 0, 32, 8, 8, 8, 256>(st);
+    add_plm_set<T, P, 3, 1, 16, 8, 8, 8, 128>(st);
     add_stage<T, P, 3, 0, 32, 8, 8, 8, 256, E, false, false>(st);
     add_stage<T, P, 3, 0, 32, 8, 8, 8, 256, E, false, true>(st);
     add_aux<T, P, 3, E>(aux);

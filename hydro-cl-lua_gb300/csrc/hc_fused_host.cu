@@ -182,9 +182,13 @@ struct FusedSet {
 static const StageLauncher* find_launcher(const FusedScheme& sch, int dim, int variant) {
     bool const plm = sch.recon == HC_RECON_PLM_CONS;
     bool const lim = sch.flux_limiter > 0;
-    for (const StageLauncher& L : stage_launchers())
-        if (L.precision == sch.precision && L.dim == dim && L.plm == plm && L.lim == lim && L.variant == variant) return &L;
-    return nullptr;
+    const StageLauncher* generic = nullptr;
+    for (const StageLauncher& L : stage_launchers()) {
+        if (L.precision != sch.precision || L.dim != dim || L.plm != plm || L.lim != lim || L.variant != variant) continue;
+        if (plm && L.slope == sch.slope_limiter) return &L;    // slope limiter compiled in
+        if (L.slope < 0) generic = &L;
+    }
+    return generic;
 }
 
 static const AuxLauncher* find_aux(int precision, int dim) {
@@ -873,7 +877,8 @@ int fused_variant(const FusedSet* f, int dim) { return f->launcher[dim - 1] ? f-
 namespace hc {
 namespace fz {
 void register_f32_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
-void register_f32_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_d2a(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_d2b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -881,7 +886,8 @@ void register_f64_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 
 void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& aux) {
     register_f32_d1(st, aux);
-    register_f32_d2(st, aux);
+    register_f32_d2a(st, aux);
+    register_f32_d2b(st, aux);
     register_f32_d3(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);

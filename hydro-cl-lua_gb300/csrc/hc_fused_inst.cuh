@@ -8,7 +8,8 @@
 namespace hc {
 namespace fz {
 
-template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM>
+template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM,
+          int SLOPE = -1>
 void add_stage(std::vector<StageLauncher>& v) {
     using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
     StageLauncher sl;
@@ -16,6 +17,7 @@ void add_stage(std::vector<StageLauncher>& v) {
     sl.dim = DIM;
     sl.plm = PLM;
     sl.lim = LIM;
+    sl.slope = SLOPE;
     sl.variant = VAR;
     sl.tx = TX;
     sl.ty = TY;
@@ -23,10 +25,10 @@ void add_stage(std::vector<StageLauncher>& v) {
     sl.nthreads = NT;
     sl.smem = Cfg::SMEM;
     sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
-        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
     };
     sl.occupancy = []() -> int {
-        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM>;
+        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE>;
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NT, Cfg::SMEM) != cudaSuccess) return -1;
@@ -38,6 +40,17 @@ void add_stage(std::vector<StageLauncher>& v) {
 inline unsigned aux_blocks(long long n) {
     long long b = (n + 255) / 256;
     return (unsigned)(b < 1 ? 1 : (b > 4096 ? 4096 : b));
+}
+
+// The FP32 PLM kernels for the slope limiters the configurations use, plus the
+// generic one: minmod, van Leer (table and comment forms), monotized central, superbee.
+template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT>
+void add_plm_set(std::vector<StageLauncher>& v) {
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MINMOD>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MONOTIZED_CENTRAL>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_SUPERBEE>(v);
 }
 
 template <typename T, int PREC, int DIM, bool EXACT>

@@ -174,70 +174,92 @@ __device__ __forceinline__ long long padIndex(const DevInst& I, int gx, int gy, 
     return (z * I.py + y) * I.px + (gx + kG);
 }
 
+// Per-tile constants: everything the sweeps and the cell epilogue need from
+// the instance, converted once per tile to the arithmetic type (FP64 work per
+// cell would run on GB300's narrow FP64 pipe).
 template <typename T>
-__device__ __forceinline__ ref::Eos refEos(const DevInst& I, int slopeLim, int fluxLim) {
-    ref::Eos e;
-    e.gamma = I.gamma; e.rhoMin = I.rhoMin; e.PMin = I.PMin;
-    e.fluxLimiter = fluxLim; e.slopeLimiter = slopeLim;
-    return e;
-}
+struct TileK {
+    fast::Eos<T> fe;      // fast form
+    ref::Eos re;          // exact form
+    T dtdx[3];            // dt / grid_dx (flux limiter)
+    double dtdx_d[3];
+    T area[3];            // areaL * invVolume per side
+    bool skip[3];         // volume <= 1e-7: the side adds nothing
+    bool zero[3];         // area <= 1e-7: zero flux
+    T invg1;              // 1 / (gamma - 1)
+    T gdx[3];             // grid_dx
+};
 
 template <typename T>
-__device__ __forceinline__ fast::Eos<T> fastEos(const DevInst& I, int slopeLim, int fluxLim) {
-    fast::Eos<T> e;
-    e.gamma = T(I.gamma);
-    e.g1 = T(I.gamma - 1.);
-    e.rhoMin = T(I.rhoMin);
-    e.PMin = T(I.PMin);
-    e.fluxLimiter = fluxLim;
-    e.slopeLimiter = slopeLim;
-    return e;
+__device__ __forceinline__ void makeTileK(TileK<T>& k, const DevInst& I, double dt, int slopeLim, int fluxLim) {
+    k.fe.gamma = T(I.gamma);
+    k.fe.g1 = T(I.gamma - 1.);
+    k.fe.rhoMin = T(I.rhoMin);
+    k.fe.PMin = T(I.PMin);
+    k.fe.fluxLimiter = fluxLim;
+    k.fe.slopeLimiter = slopeLim;
+    k.re.gamma = I.gamma;
+    k.re.rhoMin = I.rhoMin;
+    k.re.PMin = I.PMin;
+    k.re.fluxLimiter = fluxLim;
+    k.re.slopeLimiter = slopeLim;
+    k.invg1 = T(1. / (I.gamma - 1.));
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        k.dtdx_d[d] = dt / I.grid_dx[d];
+        k.dtdx[d] = T(k.dtdx_d[d]);
+        k.area[d] = T(I.area[d]);
+        k.skip[d] = I.skipDeriv[d] != 0;
+        k.zero[d] = I.zeroFlux[d] != 0;
+        k.gdx[d] = T(I.grid_dx[d]);
+    }
 }
 
 // constrainU of one cell (global frame, 5 components).
 template <typename T, bool EXACT>
-__device__ __forceinline__ void constrainCell(T* u, const DevInst& I) {
-    if (EXACT) {
+__device__ __forceinline__ void constrainCell(T* u, const TileK<T>& K) {
+    if constexpr (EXACT) {
         double U[6] = {(double)u[0], (double)u[1], (double)u[2], (double)u[3], (double)u[4], 0.};
-        ref::constrain(U, refEos<T>(I, 0, 0));
+        ref::constrain(U, K.re);
         for (int j = 0; j < 5; ++j) u[j] = (T)U[j];
     } else {
-        T const rhoMin = T(I.rhoMin), PMin = T(I.PMin), g1 = T(I.gamma - 1.);
+        T const rhoMin = K.fe.rhoMin;
         if (u[0] < rhoMin) u[0] = rhoMin;
         T const inv = fast::M<T>::rcp(u[0]);
         T const vx = u[1] * inv, vy = u[2] * inv, vz = u[3] * inv;
         T const m2 = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
-        T P = u[0] < rhoMin ? T(0) : g1 * (u[4] - T(.5) * m2 * inv);
-        if (P < PMin) P = PMin;
+        T P = u[0] < rhoMin ? T(0) : K.fe.g1 * (u[4] - T(.5) * m2 * inv);
+        if (P < K.fe.PMin) P = K.fe.PMin;
         T const rho = u[0];
         u[1] = vx * rho;
         u[2] = vy * rho;
         u[3] = vz * rho;
-        u[4] = rho * (T(.5) * (vx * vx + vy * vy + vz * vz)) + fast::M<T>::div(P, g1);
+        u[4] = rho * (T(.5) * (vx * vx + vy * vy + vz * vz)) + P * K.invg1;
     }
 }
 
-// calcDTCell of one cell (global frame).
+// calcDTCell of one cell (global frame).  The minimum over cells is exact in
+// any precision; the cross-CTA reduction is done on the FP64 bits.
 template <typename T, bool EXACT, int DIM>
-__device__ __forceinline__ double dtCell(const T* u, const DevInst& I) {
-    if (EXACT) {
+__device__ __forceinline__ T dtCell(const T* u, const TileK<T>& K, const DevInst& I) {
+    if constexpr (EXACT) {
         double U[6] = {(double)u[0], (double)u[1], (double)u[2], (double)u[3], (double)u[4], 0.};
-        return ref::dtCell(U, refEos<T>(I, 0, 0), DIM, I.grid_dx);
+        return (T)ref::dtCell(U, K.re, DIM, I.grid_dx);
     } else {
-        T const rhoMin = T(I.rhoMin), PMin = T(I.PMin), g1 = T(I.gamma - 1.);
+        T const rhoMin = K.fe.rhoMin;
         T const inv = fast::M<T>::rcp(u[0]);
         T const m2 = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
-        T const P = u[0] < rhoMin ? T(0) : g1 * (u[4] - T(.5) * m2 * inv);
-        T const Cs = P <= PMin ? T(0) : (u[0] < rhoMin ? fast::M<T>::inf() : fast::M<T>::sqrt_(T(I.gamma) * P * inv));
+        T const P = u[0] < rhoMin ? T(0) : K.fe.g1 * (u[4] - T(.5) * m2 * inv);
+        T const Cs = P <= K.fe.PMin ? T(0) : (u[0] < rhoMin ? fast::M<T>::inf() : fast::M<T>::sqrt_(K.fe.gamma * P * inv));
         T dt = fast::M<T>::inf();
 #pragma unroll
         for (int side = 0; side < DIM; ++side) {
             T const vn = u[0] < rhoMin ? T(0) : u[1 + side] * inv;
             T a = fast::tmax(fabs(vn - Cs), fabs(vn + Cs));
             a = fast::tmax(T(1e-9), a);
-            dt = fast::tmin(dt, fast::M<T>::div(T(I.grid_dx[side]), a));
+            dt = fast::tmin(dt, fast::M<T>::div(K.gdx[side], a));
         }
-        return (double)dt;
+        return dt;
     }
 }
 
@@ -288,28 +310,26 @@ struct BoxGeom {
     static constexpr int BZ = DIM > 2 ? TZ + 4 : 1;
     static constexpr int BOXN = BX * BY * BZ;
     static constexpr int DPX = TX + 1;
-    static constexpr int DN = DIM > 1 ? DPX * TY * (DIM > 2 ? TZ : 1) : 0;
-    static constexpr int STRIDE[3] = {1, BX, BX * BY};
+    static constexpr int DN = DPX * (DIM > 1 ? TY : 1) * (DIM > 2 ? TZ : 1);
 };
 
 // Sweeps one segment of L cells along AXIS.  `base` is the box index of the
 // segment's first cell.  emit(k, FL, FR) receives, for cell k of the segment,
 // its left and right face fluxes in the global frame (5 components).
 template <typename T, int AXIS, int STRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, int SLOPE, class Emit>
-__device__ __forceinline__ void sweepSegment(const T* box, int base, const DevInst& I, int slopeLimRT, int fluxLim,
-                                             double dt, Emit&& emit) {
-    // SLOPE >= 0 fixes the slope limiter at compile time; -1 dispatches on slopeLimRT
-    int const slopeLim = SLOPE >= 0 ? SLOPE : slopeLimRT;
+__device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK<T>& K, Emit&& emit) {
+    // SLOPE >= 0 fixes the slope limiter at compile time; -1 dispatches at run time
+    int const slopeLim = SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter;
     if constexpr (EXACT) {
-        ref::Eos const e = refEos<T>(I, slopeLim, fluxLim);
-        double const dt_dx = dt / I.grid_dx[AXIS];
+        ref::Eos const& e = K.re;
+        double const dt_dx = K.dtdx_d[AXIS];
         auto load = [&](int k, double* U) {
 #pragma unroll
             for (int f = 0; f < 5; ++f) U[f] = (double)box[f * BOXN + base + k * STRIDE];
             U[5] = 0.;
         };
         double Fprev[6], F[6];
-        bool const zero = I.zeroFlux[AXIS] != 0;
+        bool const zero = K.zero[AXIS];
         auto flux = [&](double* out, const double* UL, const double* UR, const ref::Iface& C,
                         const ref::Iface* IL, const ref::Iface* IR) {
             if (zero) { for (int j = 0; j < 6; ++j) out[j] = 0.; return; }
@@ -362,8 +382,8 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const DevIn
         }
     } else {
         using C5 = fast::C5<T>;
-        fast::Eos<T> const e = fastEos<T>(I, slopeLim, fluxLim);
-        T const dt_dx = T(dt / I.grid_dx[AXIS]);
+        fast::Eos<T> const& e = K.fe;
+        T const dt_dx = K.dtdx[AXIS];
         constexpr int A1 = 1 + AXIS, A2 = 1 + (AXIS + 1) % 3, A3 = 1 + (AXIS + 2) % 3;
         // loads in the interface frame (rho, m_n, m_t1, m_t2, E)
         auto load = [&](int k, C5& U) {
@@ -374,7 +394,7 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const DevIn
             U.u[3] = box[A3 * BOXN + i];
             U.u[4] = box[4 * BOXN + i];
         };
-        bool const zero = I.zeroFlux[AXIS] != 0;
+        bool const zero = K.zero[AXIS];
         // flux in the interface frame, then back to the global frame
         T Fprev[5], F[5];
         auto flux = [&](T* out, const C5& UL, const C5& UR, const fast::IfaceF<T>& C,
@@ -526,6 +546,8 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
 
         double const dt = ctl->dt;
         int const nx = I.n[0], ny = I.n[1], nz = I.n[2];
+        TileK<T> K;
+        makeTileK<T>(K, I, dt, slopeLim, fluxLim);
 
         // ---- all axes but the last: flux differences into D ----------------
         if constexpr (DIM >= 2) {
@@ -534,8 +556,8 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                 if (axis == 0) {
                     constexpr int nlines = TY * (DIM > 2 ? TZ : 1);
                     constexpr int nseg = TX / L;
-                    double const ar = I.area[0];
-                    bool const skip = I.skipDeriv[0] != 0;
+                    T const ar = K.area[0];
+                    bool const skip = K.skip[0];
                     for (int t = tid; t < nlines * nseg; t += NT) {
                         int const line = t % nlines, seg = t / nlines;
                         int const cy = line % TY, cz = line / TY;
@@ -543,12 +565,12 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                         if (x0 + cx0 >= nx || y0 + cy >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + (DIM > 2 ? 2 : 0)) * G::BY + (cy + 2)) * G::BX + (cx0 + 2);
                         T* Dl = D + (cz * TY + cy) * G::DPX + cx0;
-                        sweepSegment<T, 0, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, I, slopeLim, fluxLim, dt,
+                        sweepSegment<T, 0, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, K,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                                 for (int f = 0; f < 5; ++f) {
                                     T d = T(0);
-                                    if (!skip) d = T(0) - (T(FR[f]) * T(ar) - T(FL[f]) * T(ar));
+                                    if (!skip) d = T(0) - (T(FR[f]) * ar - T(FL[f]) * ar);
                                     Dl[f * G::DN + k] = d;
                                 }
                             });
@@ -557,8 +579,8 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                     // axis 1 of a 3D tile
                     constexpr int nlines = TX * TZ;
                     constexpr int nseg = TY / L;
-                    double const ar = I.area[1];
-                    bool const skip = I.skipDeriv[1] != 0;
+                    T const ar = K.area[1];
+                    bool const skip = K.skip[1];
                     for (int t = tid; t < nlines * nseg; t += NT) {
                         int const cx = t % TX, rest = t / TX;
                         int const cz = rest % TZ, seg = rest / TZ;
@@ -566,12 +588,12 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                         if (x0 + cx >= nx || y0 + cy0 >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + 2) * G::BY + (cy0 + 2)) * G::BX + (cx + 2);
                         T* Dl = D + (cz * TY + cy0) * G::DPX + cx;
-                        sweepSegment<T, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, I, slopeLim, fluxLim, dt,
+                        sweepSegment<T, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, K,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                                 for (int f = 0; f < 5; ++f) {
                                     T& d = Dl[f * G::DN + k * G::DPX];
-                                    if (!skip) d = d - (T(FR[f]) * T(ar) - T(FL[f]) * T(ar));
+                                    if (!skip) d = d - (T(FR[f]) * ar - T(FL[f]) * ar);
                                 }
                             });
                     }
@@ -580,25 +602,28 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             }
         }
 
-        // ---- last axis: finish each cell ------------------------------------
+        // ---- last axis: sweep into D, then finish each of the segment's cells
         constexpr int AX = DIM - 1;
         constexpr int TA = AX == 0 ? TX : (AX == 1 ? TY : TZ);
         constexpr int nlines = (TX * TY * TZ) / TA / (DIM < 2 ? TY : 1) / (DIM < 3 ? TZ : 1);
         constexpr int nseg = TA / L;
         constexpr int STRIDE_AX = AX == 0 ? 1 : (AX == 1 ? G::BX : G::BX * G::BY);
+        constexpr int DSTRIDE_AX = AX == 0 ? 1 : (AX == 1 ? G::DPX : G::DPX * TY);
 
         // stage coefficients (the reference casts beta * dt to real)
         T calpha[4], cbeta[4];
+#pragma unroll
         for (int k = 0; k < 4; ++k) {
             calpha[k] = k < st.n_alpha ? T(st.alpha[k]) : T(0);
             cbeta[k] = k < st.n_beta ? T(st.beta[k] * dt) : T(0);
         }
         T const cbcur = T(st.beta_cur * dt);
+        bool const useCur = st.beta_cur != 0.;
         T* out = reinterpret_cast<T*>(I.buf[slotBuf(st.out_buf, rot, a.rot_buf)]);
         T* dstore = st.store_deriv >= 0 ? reinterpret_cast<T*>(I.dbuf[st.store_deriv]) : nullptr;
-        double const ar = I.area[AX];
-        bool const skip = I.skipDeriv[AX] != 0;
-        double dtmin = __longlong_as_double((long long)kInfBits);
+        T const arF = K.area[AX];
+        bool const skipF = K.skip[AX];
+        T dtmin = fast::M<T>::inf();
         bool bad = false;
 
         for (int t = tid; t < nlines * nseg; t += NT) {
@@ -611,64 +636,76 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             int const gx0 = x0 + c0[0], gy0 = y0 + c0[1], gz0 = z0 + c0[2];
             if (gx0 >= nx || gy0 >= ny || gz0 >= nz) continue;
             int const base = ((c0[2] + (DIM > 2 ? 2 : 0)) * G::BY + (c0[1] + (DIM > 1 ? 2 : 0))) * G::BX + (c0[0] + 2);
-            int const dbase = (c0[2] * TY + c0[1]) * G::DPX + c0[0];
-            sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, I, slopeLim, fluxLim, dt,
+            T* Dl = D + (c0[2] * TY + c0[1]) * G::DPX + c0[0];
+            sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, K,
                 [&](int k, const auto* FL, const auto* FR) {
-                    int g[3] = {gx0, gy0, gz0};
-                    g[AX] += k;
-                    if (g[AX] >= I.n[AX]) return;
-                    T u[5], deriv[5];
 #pragma unroll
                     for (int f = 0; f < 5; ++f) {
-                        T d = DIM > 1 ? D[f * G::DN + dbase + k * (AX == 1 ? G::DPX : (AX == 2 ? G::DPX * TY : 1))] : T(0);
-                        if (!skip) d = d - (T(FR[f]) * T(ar) - T(FL[f]) * T(ar));
-                        deriv[f] = d;
+                        T& d = Dl[f * G::DN + k * DSTRIDE_AX];
+                        T dv = DIM > 1 ? d : T(0);
+                        if (!skipF) dv = dv - (T(FR[f]) * arF - T(FL[f]) * arF);
+                        d = dv;
                     }
-                    long long const idx = padIndex<DIM>(I, g[0], g[1], g[2]);
-                    // u = sum alpha_k u^(k) + sum (beta_k dt) L(u^(k)) + (beta_cur dt) deriv
-#pragma unroll
-                    for (int f = 0; f < 5; ++f) u[f] = T(0);
-                    for (int m = 0; m < st.n_alpha; ++m) {
-                        int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
-                        if (b == inBuf) {
-#pragma unroll
-                            for (int f = 0; f < 5; ++f) u[f] = u[f] + box[f * G::BOXN + base + k * STRIDE_AX] * calpha[m];
-                        } else {
-                            const T* src = reinterpret_cast<const T*>(I.buf[b]);
-#pragma unroll
-                            for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * calpha[m];
-                        }
-                    }
-                    for (int m = 0; m < st.n_beta; ++m) {
-                        const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
-#pragma unroll
-                        for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * cbeta[m];
-                    }
-                    if (st.beta_cur != 0.) {
-#pragma unroll
-                        for (int f = 0; f < 5; ++f) u[f] = u[f] + deriv[f] * cbcur;
-                    }
-                    constrainCell<T, EXACT>(u, I);
-#pragma unroll
-                    for (int f = 0; f < 5; ++f) {
-                        out[f * I.plane + idx] = u[f];
-                        bad |= !isfinite(u[f]);
-                    }
-                    scatterGhosts<T, DIM>(I, out, g[0], g[1], g[2], u);
-                    if (dstore) {
-#pragma unroll
-                        for (int f = 0; f < 5; ++f) dstore[f * I.plane + idx] = deriv[f];
-                    }
-                    if (st.last) dtmin = fmin(dtmin, dtCell<T, EXACT, DIM>(u, I));
                 });
+            // the cells of this segment: Runge-Kutta combination, constrainU,
+            // store, ghost copies, stored derivative, CFL dt
+            int const gA0 = AX == 0 ? gx0 : (AX == 1 ? gy0 : gz0);
+            int const nA = AX == 0 ? nx : (AX == 1 ? ny : nz);
+            int const kmax = nA - gA0 < L ? nA - gA0 : L;
+#pragma unroll 1
+            for (int k = 0; k < kmax; ++k) {
+                int g[3] = {gx0, gy0, gz0};
+                g[AX] += k;
+                long long const idx = padIndex<DIM>(I, g[0], g[1], g[2]);
+                T u[5], deriv[5];
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    deriv[f] = Dl[f * G::DN + k * DSTRIDE_AX];
+                    u[f] = T(0);
+                }
+                // u = sum alpha_k u^(k) + sum (beta_k dt) L(u^(k)) + (beta_cur dt) deriv
+                for (int m = 0; m < st.n_alpha; ++m) {
+                    int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
+                    if (b == inBuf) {
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) u[f] = u[f] + box[f * G::BOXN + base + k * STRIDE_AX] * calpha[m];
+                    } else {
+                        const T* src = reinterpret_cast<const T*>(I.buf[b]);
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * calpha[m];
+                    }
+                }
+                for (int m = 0; m < st.n_beta; ++m) {
+                    const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * cbeta[m];
+                }
+                if (useCur) {
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) u[f] = u[f] + deriv[f] * cbcur;
+                }
+                constrainCell<T, EXACT>(u, K);
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    out[f * I.plane + idx] = u[f];
+                    bad |= !isfinite(u[f]);
+                }
+                scatterGhosts<T, DIM>(I, out, g[0], g[1], g[2], u);
+                if (dstore) {
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) dstore[f * I.plane + idx] = deriv[f];
+                }
+                if (st.last) dtmin = fast::tmin(dtmin, dtCell<T, EXACT, DIM>(u, K, I));
+            }
         }
 
         // one FP64 atomicMin per warp for the next step's CFL dt
         if (st.last) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) dtmin = fmin(dtmin, __shfl_xor_sync(0xffffffffu, dtmin, o));
-            if ((tid & 31) == 0 && dtmin < __longlong_as_double((long long)kInfBits))
-                atomicMin(&ctl->dtmin[ctl->par ^ 1], (unsigned long long)__double_as_longlong(dtmin));
+            for (int o = 16; o > 0; o >>= 1) dtmin = fast::tmin(dtmin, __shfl_xor_sync(0xffffffffu, dtmin, o));
+            double const m = (double)dtmin;
+            if ((tid & 31) == 0 && m < __longlong_as_double((long long)kInfBits))
+                atomicMin(&ctl->dtmin[ctl->par ^ 1], (unsigned long long)__double_as_longlong(m));
         }
         if (__any_sync(0xffffffffu, bad) && (tid & 31) == 0) atomicOr(&ctl->status, DEV_NONFINITE);
         __syncthreads();
@@ -704,6 +741,8 @@ __global__ void k_fill_ghosts(const DevInst* inst, int slot, int buf) {
 template <typename T, int DIM, bool EXACT>
 __global__ void k_constrain(const DevInst* inst, int slot, int buf) {
     const DevInst& I = inst[slot];
+    TileK<T> K;
+    makeTileK<T>(K, I, 0., 0, 0);
     T* base = reinterpret_cast<T*>(I.buf[buf]);
     long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
@@ -711,7 +750,7 @@ __global__ void k_constrain(const DevInst* inst, int slot, int buf) {
         long long const idx = padIndex<DIM>(I, gx, gy, gz);
         T u[5];
         for (int f = 0; f < 5; ++f) u[f] = base[f * I.plane + idx];
-        constrainCell<T, EXACT>(u, I);
+        constrainCell<T, EXACT>(u, K);
         for (int f = 0; f < 5; ++f) base[f * I.plane + idx] = u[f];
     }
 }
@@ -720,6 +759,8 @@ __global__ void k_constrain(const DevInst* inst, int slot, int buf) {
 template <typename T, int DIM, bool EXACT>
 __global__ void k_calc_dt(const DevInst* inst, DevCtl* ctl, int slot, int buf) {
     const DevInst& I = inst[slot];
+    TileK<T> K;
+    makeTileK<T>(K, I, 0., 0, 0);
     const T* base = reinterpret_cast<const T*>(I.buf[buf]);
     long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
     double m = __longlong_as_double((long long)kInfBits);
@@ -728,7 +769,7 @@ __global__ void k_calc_dt(const DevInst* inst, DevCtl* ctl, int slot, int buf) {
         long long const idx = padIndex<DIM>(I, gx, gy, gz);
         T u[5];
         for (int f = 0; f < 5; ++f) u[f] = base[f * I.plane + idx];
-        m = fmin(m, dtCell<T, EXACT, DIM>(u, I));
+        m = fmin(m, (double)dtCell<T, EXACT, DIM>(u, K, I));
     }
     for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0 && m < __longlong_as_double((long long)kInfBits))

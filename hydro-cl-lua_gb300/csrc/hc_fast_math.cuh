@@ -29,12 +29,16 @@ namespace fast {
 
 template <typename T> struct M;
 template <> struct M<float> {
+    static __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
+    static __device__ __forceinline__ bool finite_(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
     static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.f, x); }
     static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
     static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
     static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
 };
 template <> struct M<double> {
+    static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
+    static __device__ __forceinline__ bool finite_(double x) { return isfinite(x); }
     static __device__ __forceinline__ double rcp(double x) { return 1. / x; }
     static __device__ __forceinline__ double div(double a, double b) { return a / b; }
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
@@ -54,8 +58,8 @@ __device__ __forceinline__ T limiter(int which, T r) {
     case 2: return r;
     case 3: return T(.5) * (one + r);
     case 4: return M<T>::div(tmax(z, r) * (T(3) * r + one), (r + one) * (r + one));
-    case 5: return tmax(z, M<T>::div(T(1.5) * (r + fabs(r)), r + two));
-    case 6: return tmax(z, M<T>::div(two * (r + fabs(r)), r + T(3)));
+    case 5: return tmax(z, M<T>::div(T(1.5) * (r + M<T>::abs_(r)), r + two));
+    case 6: return tmax(z, M<T>::div(two * (r + M<T>::abs_(r)), r + T(3)));
     case 7: return tmax(z, tmin(two * r, tmin(M<T>::div(one + two * r, T(3)), two)));
     case 8: return tmax(z, tmin(r, one));
     case 9: return tmax(z, tmin(r, T(1.5)));
@@ -69,7 +73,7 @@ __device__ __forceinline__ T limiter(int which, T r) {
     case 17: return tmax(z, tmin(two, tmin(T(.5) * (one + r), two * r)));
     case 18: return tmax(z, tmax(tmin(one, two * r), tmin(two, r)));
     case 19: return T(.5) * (r + one) * tmin(one, tmin(M<T>::div(T(4) * r, r + one), M<T>::div(T(4), r + one)));
-    case 20: return M<T>::div(r + fabs(r), one + fabs(r));
+    case 20: return M<T>::div(r + M<T>::abs_(r), one + M<T>::abs_(r));
     }
     return z;
 }

@@ -188,6 +188,8 @@ struct TileK {
     bool zero[3];         // area <= 1e-7: zero flux
     T invg1;              // 1 / (gamma - 1)
     T gdx[3];             // grid_dx
+    T calpha[4], cbeta[4], cbcur;   // stage coefficients (beta * dt cast to real, as the reference does)
+    bool useCur;
 };
 
 template <typename T>
@@ -255,7 +257,7 @@ __device__ __forceinline__ T dtCell(const T* u, const TileK<T>& K, const DevInst
 #pragma unroll
         for (int side = 0; side < DIM; ++side) {
             T const vn = u[0] < rhoMin ? T(0) : u[1 + side] * inv;
-            T a = fast::tmax(fabs(vn - Cs), fabs(vn + Cs));
+            T a = fast::tmax(fast::M<T>::abs_(vn - Cs), fast::M<T>::abs_(vn + Cs));
             a = fast::tmax(T(1e-9), a);
             dt = fast::tmin(dt, fast::M<T>::div(K.gdx[side], a));
         }
@@ -490,7 +492,8 @@ template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT>
 struct StageCfg {
     using G = BoxGeom<DIM, TX, TY, TZ>;
     static constexpr size_t kBarOff = (((size_t)(5 * G::BOXN + 5 * G::DN) * sizeof(T)) + 15) / 16 * 16;
-    static constexpr size_t SMEM = kBarOff + 16;
+    static constexpr size_t kKOff = kBarOff + 16;
+    static constexpr size_t SMEM = kKOff + (sizeof(TileK<T>) + 15) / 16 * 16;
     static constexpr unsigned BYTES = (unsigned)(5 * G::BOXN * sizeof(T));
     static_assert(G::BX <= 256 && G::BY <= 256 && G::BZ <= 256, "TMA box extent");
     static_assert((G::BX * sizeof(T)) % 16 == 0, "TMA box rows must be a multiple of 16 bytes");
@@ -507,6 +510,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
     T* box = reinterpret_cast<T*>(smem);
     T* D = box + 5 * G::BOXN;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Cfg::kBarOff);
+    TileK<T>* Ks = reinterpret_cast<TileK<T>*>(smem + Cfg::kKOff);
     int const tid = threadIdx.x;
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -534,6 +538,16 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             if (DIM == 1) tma_load<2>(box, map, x0, 0, 0, 0, bar);
             else if (DIM == 2) tma_load<3>(box, map, x0, y0, 0, 0, bar);
             else tma_load<4>(box, map, x0, y0, z0, 0, bar);
+            // while the tile streams in: the tile's constants, once, in FP64
+            double const dt = ctl->dt;
+            makeTileK<T>(*Ks, I, dt, slopeLim, fluxLim);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                Ks->calpha[k] = k < st.n_alpha ? T(st.alpha[k]) : T(0);
+                Ks->cbeta[k] = k < st.n_beta ? T(st.beta[k] * dt) : T(0);
+            }
+            Ks->cbcur = T(st.beta_cur * dt);
+            Ks->useCur = st.beta_cur != 0.;
         }
         if (!mbar_wait_bounded(bar, phase, kSpinLimit)) {
             // the copy did not complete: record it, give the copy a second
@@ -543,11 +557,10 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             return;
         }
         phase ^= 1u;
+        __syncthreads();   // the tile constants are in shared memory
 
-        double const dt = ctl->dt;
         int const nx = I.n[0], ny = I.n[1], nz = I.n[2];
-        TileK<T> K;
-        makeTileK<T>(K, I, dt, slopeLim, fluxLim);
+        TileK<T> const& K = *Ks;
 
         // ---- all axes but the last: flux differences into D ----------------
         if constexpr (DIM >= 2) {
@@ -610,15 +623,8 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
         constexpr int STRIDE_AX = AX == 0 ? 1 : (AX == 1 ? G::BX : G::BX * G::BY);
         constexpr int DSTRIDE_AX = AX == 0 ? 1 : (AX == 1 ? G::DPX : G::DPX * TY);
 
-        // stage coefficients (the reference casts beta * dt to real)
-        T calpha[4], cbeta[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            calpha[k] = k < st.n_alpha ? T(st.alpha[k]) : T(0);
-            cbeta[k] = k < st.n_beta ? T(st.beta[k] * dt) : T(0);
-        }
-        T const cbcur = T(st.beta_cur * dt);
-        bool const useCur = st.beta_cur != 0.;
+        T const cbcur = K.cbcur;
+        bool const useCur = K.useCur;
         T* out = reinterpret_cast<T*>(I.buf[slotBuf(st.out_buf, rot, a.rot_buf)]);
         T* dstore = st.store_deriv >= 0 ? reinterpret_cast<T*>(I.dbuf[st.store_deriv]) : nullptr;
         T const arF = K.area[AX];
@@ -668,17 +674,17 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                     int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
                     if (b == inBuf) {
 #pragma unroll
-                        for (int f = 0; f < 5; ++f) u[f] = u[f] + box[f * G::BOXN + base + k * STRIDE_AX] * calpha[m];
+                        for (int f = 0; f < 5; ++f) u[f] = u[f] + box[f * G::BOXN + base + k * STRIDE_AX] * K.calpha[m];
                     } else {
                         const T* src = reinterpret_cast<const T*>(I.buf[b]);
 #pragma unroll
-                        for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * calpha[m];
+                        for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * K.calpha[m];
                     }
                 }
                 for (int m = 0; m < st.n_beta; ++m) {
                     const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
 #pragma unroll
-                    for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * cbeta[m];
+                    for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * K.cbeta[m];
                 }
                 if (useCur) {
 #pragma unroll
@@ -688,7 +694,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
                     out[f * I.plane + idx] = u[f];
-                    bad |= !isfinite(u[f]);
+                    bad |= !fast::M<T>::finite_(u[f]);
                 }
                 scatterGhosts<T, DIM>(I, out, g[0], g[1], g[2], u);
                 if (dstore) {

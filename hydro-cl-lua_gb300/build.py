@@ -31,6 +31,7 @@ SOURCES = {
     "hc_fused_f32_d1.cu": FAST,
     "hc_fused_f32_d2a.cu": FAST,
     "hc_fused_f32_d2b.cu": FAST,
+    "hc_fused_f32_d2c.cu": FAST,
     "hc_fused_f32_d3.cu": FAST,
     "hc_fused_f64_d1.cu": EXACT,
     "hc_fused_f64_d2.cu": EXACT,

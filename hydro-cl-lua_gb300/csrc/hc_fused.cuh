@@ -318,7 +318,10 @@ struct BoxGeom {
 // Sweeps one segment of L cells along AXIS.  `base` is the box index of the
 // segment's first cell.  emit(k, FL, FR) receives, for cell k of the segment,
 // its left and right face fluxes in the global frame (5 components).
-template <typename T, int AXIS, int STRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, int SLOPE, class Emit>
+// UNR: unroll factor of the sliding-window loop (0: fully unrolled).  Full
+// unrolling removes the window copies; partial unrolling keeps the code
+// footprint inside the instruction cache.
+template <typename T, int AXIS, int STRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, int SLOPE, int UNR, class Emit>
 __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK<T>& K, Emit&& emit) {
     // SLOPE >= 0 fixes the slope limiter at compile time; -1 dispatches at run time
     int const slopeLim = SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter;
@@ -414,7 +417,7 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
             C5 Um, U0, Up, prevR, fL, fR;
             load(-2, Um);
             load(-1, U0);
-#pragma unroll
+#pragma unroll (UNR == 0 ? L + 2 : UNR)
             for (int k = -1; k <= L; ++k) {
                 load(k + 1, Up);
 #pragma unroll
@@ -464,7 +467,7 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
         } else {
             C5 Ua, Ub;
             load(-1, Ua);
-#pragma unroll
+#pragma unroll (UNR == 0 ? L + 1 : UNR)
             for (int k = 0; k <= L; ++k) {
                 load(k, Ub);
                 T Fr[5];
@@ -502,7 +505,7 @@ struct StageCfg {
 
 constexpr unsigned kSpinLimit = 1u << 22;
 
-template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM, int SLOPE>
+template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM, int SLOPE, int UNR>
 __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs a, int slopeLim, int fluxLim) {
     using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
     using G = typename Cfg::G;
@@ -578,7 +581,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                         if (x0 + cx0 >= nx || y0 + cy >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + (DIM > 2 ? 2 : 0)) * G::BY + (cy + 2)) * G::BX + (cx0 + 2);
                         T* Dl = D + (cz * TY + cy) * G::DPX + cx0;
-                        sweepSegment<T, 0, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, K,
+                        sweepSegment<T, 0, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                                 for (int f = 0; f < 5; ++f) {
@@ -601,7 +604,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                         if (x0 + cx >= nx || y0 + cy0 >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + 2) * G::BY + (cy0 + 2)) * G::BX + (cx + 2);
                         T* Dl = D + (cz * TY + cy0) * G::DPX + cx;
-                        sweepSegment<T, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, K,
+                        sweepSegment<T, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                                 for (int f = 0; f < 5; ++f) {
@@ -643,7 +646,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             if (gx0 >= nx || gy0 >= ny || gz0 >= nz) continue;
             int const base = ((c0[2] + (DIM > 2 ? 2 : 0)) * G::BY + (c0[1] + (DIM > 1 ? 2 : 0))) * G::BX + (c0[0] + 2);
             T* Dl = D + (c0[2] * TY + c0[1]) * G::DPX + c0[0];
-            sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM, SLOPE>(box, base, K,
+            sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K,
                 [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                     for (int f = 0; f < 5; ++f) {

@@ -177,6 +177,7 @@ struct FusedSet {
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
     int graph_dims_mask = 0;
+    std::string tune_log;          // per-variant timings of the last autotune
 };
 
 static const StageLauncher* find_launcher(const FusedScheme& sch, int dim, int variant) {
@@ -805,9 +806,14 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
     std::map<std::string, int> cache;
     if (cache_path) {
         std::ifstream in(cache_path);
-        std::string k;
-        int v;
-        while (in >> k >> v) cache[k] = v;
+        std::string line;
+        while (std::getline(in, line)) {
+            if (line.empty() || line[0] == '#') continue;
+            std::istringstream ls(line);
+            std::string k;
+            int v;
+            if (ls >> k >> v) cache[k] = v;
+        }
     }
     HC_CUDA(cudaStreamSynchronize(f->stream));
     for (int dim = 1; dim <= 3; ++dim) {
@@ -825,6 +831,7 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
         }
         int best = 0;
         float bestMs = 1e30f;
+        std::ostringstream log;
         for (int v = 0; v < 16; ++v) {
             if (!find_launcher(f->sch, dim, v)) continue;
             HC_CHECK(set_launcher(f, dim, v));
@@ -854,8 +861,11 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
             cudaEventDestroy(e1);
             fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0);
             HC_CUDA(cudaStreamSynchronize(f->stream));
+            log << "# " << key << " variant " << v << " tile " << f->launcher[dim - 1]->tx << "x" << f->launcher[dim - 1]->ty
+                << "x" << f->launcher[dim - 1]->tz << " threads " << f->launcher[dim - 1]->nthreads << " ms/stage " << ms / reps << "\n";
             if (ms < bestMs) { bestMs = ms; best = v; }
         }
+        f->tune_log += log.str();
         HC_CHECK(set_launcher(f, dim, best));
         reencode_all(f, dim);
         f->items_dirty = true;
@@ -866,6 +876,7 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
     if (cache_path) {
         std::ofstream out(cache_path);
         for (auto& kv : cache) out << kv.first << " " << kv.second << "\n";
+        out << f->tune_log;
     }
     return fused_sync(f);
 }
@@ -879,6 +890,7 @@ namespace fz {
 void register_f32_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2a(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_d2c(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -888,6 +900,7 @@ void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>
     register_f32_d1(st, aux);
     register_f32_d2a(st, aux);
     register_f32_d2b(st, aux);
+    register_f32_d2c(st, aux);
     register_f32_d3(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);

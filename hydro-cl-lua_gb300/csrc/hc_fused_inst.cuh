@@ -9,7 +9,7 @@ namespace hc {
 namespace fz {
 
 template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM,
-          int SLOPE = -1>
+          int SLOPE = -1, int UNR = 0>
 void add_stage(std::vector<StageLauncher>& v) {
     using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
     StageLauncher sl;
@@ -25,10 +25,10 @@ void add_stage(std::vector<StageLauncher>& v) {
     sl.nthreads = NT;
     sl.smem = Cfg::SMEM;
     sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
-        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
     };
     sl.occupancy = []() -> int {
-        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE>;
+        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR>;
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NT, Cfg::SMEM) != cudaSuccess) return -1;
@@ -43,14 +43,22 @@ inline unsigned aux_blocks(long long n) {
 }
 
 // The FP32 PLM kernels for the slope limiters the configurations use, plus the
-// generic one: minmod, van Leer (table and comment forms), monotized central, superbee.
-template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT>
+// generic one: minmod, van Leer (comment form), monotized central, superbee.
+template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, int UNR = 0>
 void add_plm_set(std::vector<StageLauncher>& v) {
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MINMOD>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MONOTIZED_CENTRAL>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_SUPERBEE>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1, UNR>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MINMOD, UNR>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MONOTIZED_CENTRAL, UNR>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS, UNR>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_SUPERBEE, UNR>(v);
+}
+
+// Extra schedules for one compiled-in limiter (the batched configuration's)
+// and the generic kernel.
+template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, int UNR>
+void add_plm_pair(std::vector<StageLauncher>& v) {
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1, UNR>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS, UNR>(v);
 }
 
 template <typename T, int PREC, int DIM, bool EXACT>

@@ -1,0 +1,84 @@
+--[[
+LuaJIT ffi binding of libhydrocuda.so: the declarations of include/hydrocuda.h
+that the 'cuda' solver class uses.  Load with
+
+	local hc = require 'hydrocuda_ffi'
+
+The library is looked up next to this file's package directory
+(hydro-cl-lua_gb300/libhydrocuda.so), then on the system path.
+--]]
+local ffi = require 'ffi'
+
+ffi.cdef[[
+typedef struct hc_solver_desc {
+	int dim;
+	int n[3];
+	double mins[3];
+	double maxs[3];
+	int boundary[6];
+	int flux_limiter;
+	int recon;
+	int slope_limiter;
+	int integrator;
+	int precision;
+	double gamma;
+	double rho_min;
+	double p_min;
+	double cfl;
+	double fixed_dt;
+} hc_solver_desc;
+typedef struct hc_context hc_context;
+typedef struct hc_solver hc_solver;
+const char* hc_version(void);
+const char* hc_last_error(void);
+int hc_context_create(int device, hc_context** out);
+int hc_context_destroy(hc_context* ctx);
+int hc_solver_create(hc_context* ctx, const hc_solver_desc* desc, hc_solver** out);
+int hc_solver_destroy(hc_solver* s);
+int hc_solver_reset_state(hc_solver* s, const void* cons, int layout);
+int hc_solver_set_state(hc_solver* s, const void* cons, int layout, int with_ghosts);
+int hc_solver_get_state(hc_solver* s, void* cons, int layout, int with_ghosts);
+int hc_solver_boundary(hc_solver* s);
+int hc_solver_constrain_u(hc_solver* s);
+int hc_solver_calc_dt(hc_solver* s, double* dt);
+int hc_solver_step(hc_solver* s, double dt);
+int hc_solver_update(hc_solver* s, double* dt_out);
+int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long long* steps_done);
+int hc_solver_get_time(hc_solver* s, double* t);
+int hc_solver_set_time(hc_solver* s, double t);
+int hc_solver_status(hc_solver* s);
+]]
+
+local here = debug.getinfo(1, 'S').source:match'^@(.*)/[^/]*$' or '.'
+local ok, lib = pcall(ffi.load, here .. '/../libhydrocuda.so')
+if not ok then lib = ffi.load'hydrocuda' end
+
+local M = {lib = lib}
+
+-- names as in hydro/app.lua:614-635 (0-based for the C ABI)
+M.limiterIndex = {}
+for i, name in ipairs{
+	'donor cell', 'Lax-Wendroff', 'Beam-Warming', 'Fromm', 'CHARM', 'HCUS', 'HQUICK', 'Koren',
+	'minmod', 'Oshker', 'ospre', 'smart', 'Sweby', 'UMIST', 'van Albada 1', 'van Albada 2',
+	'van Leer', 'monotized central', 'superbee', 'Barth-Jespersen', 'van Leer (abs)',
+} do M.limiterIndex[name] = i - 1 end
+
+M.integratorIndex = {}
+for i, name in ipairs{
+	'forward Euler', 'Runge-Kutta 2', 'Runge-Kutta 2 Heun', 'Runge-Kutta 2 Ralston', 'Runge-Kutta 3',
+	'Runge-Kutta 4', 'Runge-Kutta 4, 3/8ths rule', 'Runge-Kutta 2, TVD', 'Runge-Kutta 2, non-TVD',
+	'Runge-Kutta 3, TVD', 'Runge-Kutta 4, TVD', 'Runge-Kutta 4, non-TVD',
+} do M.integratorIndex[name] = i - 1 end
+
+M.boundaryIndex = {none = 0, periodic = 1, mirror = 2, freeflow = 3}
+M.reconIndex = {['piecewise constant'] = 1, ['plm cons'] = 2}
+M.precisionIndex = {['f64 plain'] = 0, f64 = 1, f32 = 2}
+M.LAYOUT_AOS6_F64 = 0
+
+function M.check(code)
+	if code ~= 0 then
+		error('libhydrocuda: '..tostring(code)..': '..ffi.string(lib.hc_last_error()), 2)
+	end
+end
+
+return M

@@ -264,5 +264,42 @@ __device__ __forceinline__ T plmSigma(T um, T u0, T up, int lim) {
     return limiter<T>(lim, r) * den;
 }
 
+// Half slope .5 * phi(r) * dU of "plm cons" for a limiter fixed at compile
+// time.  For the symmetric limiters (phi(r) = r phi(1/r)) the reference's
+// selector between r = dUL/dUR and r = dUR/dUL (plm.cl:62-71) picks the same
+// value either way, and phi(r) dU has a closed form in dUL and dUR that needs
+// neither r nor the selector; all are zero unless dUL dUR > 0:
+//   minmod             the one of dUL, dUR smaller in magnitude
+//   monotized central  sign * min(2|dUL|, |dUL + dUR| / 2, 2|dUR|)
+//   superbee           sign * max(min(|dUR|, 2|dUL|), min(2|dUR|, |dUL|))
+//   van Leer (abs)     2 dUL dUR / (dUL + dUR)
+// The table's van Leer keeps the general path: its 0/0 at r = -1 is behaviour
+// the reference has.
+template <typename T, int LIMC>
+__device__ __forceinline__ T plmHalfSlope(T um, T u0, T up, int limRT) {
+    T const dUR = up - u0;
+    T const dUL = u0 - um;
+    if constexpr (LIMC == 8 || LIMC == 17 || LIMC == 18 || LIMC == 20) {
+        T const prod = dUL * dUR;
+        T h;
+        if constexpr (LIMC == 8) {
+            h = T(.5) * (M<T>::abs_(dUL) < M<T>::abs_(dUR) ? dUL : dUR);
+        } else if constexpr (LIMC == 17) {
+            T const a = M<T>::abs_(dUL), b = M<T>::abs_(dUR);
+            T const m = tmin(tmin(a, b), T(.25) * M<T>::abs_(dUL + dUR));
+            h = dUR < T(0) ? -m : m;
+        } else if constexpr (LIMC == 18) {
+            T const a = M<T>::abs_(dUL), b = M<T>::abs_(dUR);
+            T const m = tmax(tmin(b, T(2) * a), tmin(T(2) * b, a));
+            h = T(.5) * (dUR < T(0) ? -m : m);
+        } else {
+            h = M<T>::div(prod, dUL + dUR);
+        }
+        return prod > T(0) ? h : T(0);
+    } else {
+        return T(.5) * plmSigma<T>(um, u0, up, LIMC >= 0 ? LIMC : limRT);
+    }
+}
+
 }  // namespace fast
 }  // namespace hc

@@ -422,7 +422,7 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
                 load(k + 1, Up);
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
-                    T const sg = T(.5) * fast::plmSigma<T>(Um.u[j], U0.u[j], Up.u[j], slopeLim);
+                    T const sg = fast::plmHalfSlope<T, SLOPE>(Um.u[j], U0.u[j], Up.u[j], slopeLim);
                     fL.u[j] = U0.u[j] - sg;
                     fR.u[j] = U0.u[j] + sg;
                 }

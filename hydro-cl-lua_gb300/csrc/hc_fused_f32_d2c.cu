@@ -1,6 +1,6 @@
-// hc_fused_f32_d2c.cu -- 2D stage kernels, FP32 (fast form): extra schedules
-// (shorter segments for more resident warps, partial unrolling for a smaller
-// code footprint) timed by the autotuner.
+// hc_fused_f32_d2c.cu -- 2D stage kernels, FP32 (fast form): further
+// schedules timed by the autotuner (segment length, unrolling, tile shape),
+// for the batched configuration's limiter and the generic one.
 #include "hc_fused_inst.cuh"
 
 namespace hc {
@@ -10,12 +10,14 @@ void register_f32_d2c(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& 
     using T = float;
     constexpr int P = HC_F32_FUSED;
     (void)aux;
-    // 4: 64x32, L 4, 512 threads; 5: 64x32, L 8, unroll 2; 6: 64x32, L 4, 512 threads, unroll 2;
-    // 7: 32x32, L 4, 256 threads
-    add_plm_pair<T, P, 2, 4, 64, 32, 1, 4, 512, 0>(st);
-    add_plm_pair<T, P, 2, 5, 64, 32, 1, 8, 256, 2>(st);
-    add_plm_pair<T, P, 2, 6, 64, 32, 1, 4, 512, 2>(st);
-    add_plm_pair<T, P, 2, 7, 32, 32, 1, 4, 256, 0>(st);
+    // 2: 64x32, segments of 8, 256 threads, unrolled by 2
+    // 3: 64x32, segments of 8, 256 threads, fully unrolled
+    // 4: 64x16, segments of 4, 256 threads
+    // 5: 32x64, segments of 4, 512 threads
+    add_plm_pair<T, P, 2, 2, 64, 32, 1, 8, 256, 2>(st);
+    add_plm_pair<T, P, 2, 3, 64, 32, 1, 8, 256, 0>(st);
+    add_plm_pair<T, P, 2, 4, 64, 16, 1, 4, 256, 0>(st);
+    add_plm_pair<T, P, 2, 5, 32, 64, 1, 4, 512, 0>(st);
 }
 
 }  // namespace fz

@@ -8,11 +8,13 @@ void register_f32_d3(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& a
     using T = float;
     constexpr int P = HC_F32_FUSED;
     constexpr bool E = false;
-    // variants: 32x8x8 (256 thr), 16x8x8 (128 thr); L = 8
-    add_plm_set<T, P, 3, 0, 32, 8, 8, 8, 256>(st);
-    add_plm_set<T, P, 3, 1, 16, 8, 8, 8, 128>(st);
-    add_stage<T, P, 3, 0, 32, 8, 8, 8, 256, E, false, false>(st);
-    add_stage<T, P, 3, 0, 32, 8, 8, 8, 256, E, false, true>(st);
+    // variants: 0: 16x8x8, segments of 4, 256 threads; 1: 32x8x8, segments of 8, 256 threads;
+    //           2: 16x8x8, segments of 8, 128 threads
+    add_plm_set<T, P, 3, 0, 16, 8, 8, 4, 256>(st);
+    add_plm_set<T, P, 3, 1, 32, 8, 8, 8, 256>(st);
+    add_plm_pair<T, P, 3, 2, 16, 8, 8, 8, 128, 0>(st);
+    add_stage<T, P, 3, 0, 16, 8, 8, 4, 256, E, false, false>(st);
+    add_stage<T, P, 3, 0, 16, 8, 8, 4, 256, E, false, true>(st);
     add_aux<T, P, 3, E>(aux);
 }
 

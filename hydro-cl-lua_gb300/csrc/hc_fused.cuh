@@ -59,6 +59,8 @@ struct DevInst {
     double gamma, rhoMin, PMin, cfl, fixed_dt, t_end;
     long long max_steps;
     int stop_on_error;     // 1 (batched solves): a non-finite state or dt ends the instance
+    // the same constants in FP32, converted once on the host
+    float f_gamma, f_g1, f_rhoMin, f_PMin, f_invg1, f_area[3], f_gdx[3];
     void* buf[kMaxBufs];
     void* dbuf[kMaxDBufs];
 };
@@ -69,13 +71,41 @@ struct DevCtl {
     long long steps;
     int active, stepping, done, status, par;
     int rot;                       // 1: state buffers 0 and StageArgs::rot_buf are swapped for this slot
+    // per-step coefficients, set when a step begins: beta * dt of each stage
+    // ([stage][term], term 4 = the stage's own derivative), dt / grid_dx
+    double cb_d[4][5];
+    float cb_f[4][5];
+    double dtdx_d[3];
+    float dtdx_f[3];
 };
 
+// beta coefficients of the integrator plan, [stage][term] as in DevCtl::cb_*
+struct BetaTable {
+    double b[4][5];
+};
+
+__device__ __forceinline__ void fillStepCoefs(DevCtl& c, const DevInst& I, const BetaTable& bt, double dt) {
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+            c.cb_d[s][m] = bt.b[s][m] * dt;
+            c.cb_f[s][m] = (float)c.cb_d[s][m];
+        }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        c.dtdx_d[d] = dt / I.grid_dx[d];
+        c.dtdx_f[d] = (float)c.dtdx_d[d];
+    }
+}
+
 struct StageDev {
+    int stage;
     int in_buf, out_buf;
     int n_alpha;
     int alpha_buf[4];
     double alpha[4];
+    float alpha_f[4];
     int n_beta;
     int beta_buf[4];
     double beta[4];
@@ -192,12 +222,24 @@ struct TileK {
     bool useCur;
 };
 
+// Fills the tile constants from the instance (host-converted) and the slot's
+// per-step coefficients: loads only, no FP64 arithmetic in the stage kernel.
 template <typename T>
-__device__ __forceinline__ void makeTileK(TileK<T>& k, const DevInst& I, double dt, int slopeLim, int fluxLim) {
-    k.fe.gamma = T(I.gamma);
-    k.fe.g1 = T(I.gamma - 1.);
-    k.fe.rhoMin = T(I.rhoMin);
-    k.fe.PMin = T(I.PMin);
+__device__ __forceinline__ void makeTileK(TileK<T>& k, const DevInst& I, const DevCtl* c, const StageDev* st,
+                                          int slopeLim, int fluxLim) {
+    if constexpr (sizeof(T) == 4) {
+        k.fe.gamma = I.f_gamma;
+        k.fe.g1 = I.f_g1;
+        k.fe.rhoMin = I.f_rhoMin;
+        k.fe.PMin = I.f_PMin;
+        k.invg1 = I.f_invg1;
+    } else {
+        k.fe.gamma = I.gamma;
+        k.fe.g1 = I.gamma - 1.;
+        k.fe.rhoMin = I.rhoMin;
+        k.fe.PMin = I.PMin;
+        k.invg1 = 1. / (I.gamma - 1.);
+    }
     k.fe.fluxLimiter = fluxLim;
     k.fe.slopeLimiter = slopeLim;
     k.re.gamma = I.gamma;
@@ -205,15 +247,29 @@ __device__ __forceinline__ void makeTileK(TileK<T>& k, const DevInst& I, double 
     k.re.PMin = I.PMin;
     k.re.fluxLimiter = fluxLim;
     k.re.slopeLimiter = slopeLim;
-    k.invg1 = T(1. / (I.gamma - 1.));
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        k.dtdx_d[d] = dt / I.grid_dx[d];
-        k.dtdx[d] = T(k.dtdx_d[d]);
-        k.area[d] = T(I.area[d]);
+        if constexpr (sizeof(T) == 4) {
+            k.area[d] = I.f_area[d];
+            k.gdx[d] = I.f_gdx[d];
+        } else {
+            k.area[d] = I.area[d];
+            k.gdx[d] = I.grid_dx[d];
+        }
         k.skip[d] = I.skipDeriv[d] != 0;
         k.zero[d] = I.zeroFlux[d] != 0;
-        k.gdx[d] = T(I.grid_dx[d]);
+        k.dtdx_d[d] = c ? c->dtdx_d[d] : 0.;
+        k.dtdx[d] = c ? (sizeof(T) == 4 ? (T)c->dtdx_f[d] : (T)c->dtdx_d[d]) : T(0);
+    }
+    if (st && c) {
+        int const s = st->stage;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            k.calpha[m] = sizeof(T) == 4 ? (T)st->alpha_f[m] : (T)st->alpha[m];
+            k.cbeta[m] = sizeof(T) == 4 ? (T)c->cb_f[s][m] : (T)c->cb_d[s][m];
+        }
+        k.cbcur = sizeof(T) == 4 ? (T)c->cb_f[s][4] : (T)c->cb_d[s][4];
+        k.useCur = st->beta_cur != 0.;
     }
 }
 
@@ -495,8 +551,7 @@ template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT>
 struct StageCfg {
     using G = BoxGeom<DIM, TX, TY, TZ>;
     static constexpr size_t kBarOff = (((size_t)(5 * G::BOXN + 5 * G::DN) * sizeof(T)) + 15) / 16 * 16;
-    static constexpr size_t kKOff = kBarOff + 16;
-    static constexpr size_t SMEM = kKOff + (sizeof(TileK<T>) + 15) / 16 * 16;
+    static constexpr size_t SMEM = kBarOff + 16;
     static constexpr unsigned BYTES = (unsigned)(5 * G::BOXN * sizeof(T));
     static_assert(G::BX <= 256 && G::BY <= 256 && G::BZ <= 256, "TMA box extent");
     static_assert((G::BX * sizeof(T)) % 16 == 0, "TMA box rows must be a multiple of 16 bytes");
@@ -513,7 +568,6 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
     T* box = reinterpret_cast<T*>(smem);
     T* D = box + 5 * G::BOXN;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Cfg::kBarOff);
-    TileK<T>* Ks = reinterpret_cast<TileK<T>*>(smem + Cfg::kKOff);
     int const tid = threadIdx.x;
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -541,17 +595,10 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             if (DIM == 1) tma_load<2>(box, map, x0, 0, 0, 0, bar);
             else if (DIM == 2) tma_load<3>(box, map, x0, y0, 0, 0, bar);
             else tma_load<4>(box, map, x0, y0, z0, 0, bar);
-            // while the tile streams in: the tile's constants, once, in FP64
-            double const dt = ctl->dt;
-            makeTileK<T>(*Ks, I, dt, slopeLim, fluxLim);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                Ks->calpha[k] = k < st.n_alpha ? T(st.alpha[k]) : T(0);
-                Ks->cbeta[k] = k < st.n_beta ? T(st.beta[k] * dt) : T(0);
-            }
-            Ks->cbcur = T(st.beta_cur * dt);
-            Ks->useCur = st.beta_cur != 0.;
         }
+        // the tile's constants (loads; no FP64 arithmetic) while the tile streams in
+        TileK<T> K;
+        makeTileK<T>(K, I, ctl, &st, slopeLim, fluxLim);
         if (!mbar_wait_bounded(bar, phase, kSpinLimit)) {
             // the copy did not complete: record it, give the copy a second
             // bounded chance to land before the CTA releases its smem, stop
@@ -560,10 +607,8 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             return;
         }
         phase ^= 1u;
-        __syncthreads();   // the tile constants are in shared memory
 
         int const nx = I.n[0], ny = I.n[1], nz = I.n[2];
-        TileK<T> const& K = *Ks;
 
         // ---- all axes but the last: flux differences into D ----------------
         if constexpr (DIM >= 2) {
@@ -727,7 +772,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
 
 // Finishes a pending step (t += dt) and begins the next one for every slot:
 // the App's exit test (t >= t_end, before stepping), then dt = cfl * min.
-__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates);
+__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates, BetaTable bt);
 
 template <typename T, int DIM>
 __global__ void k_fill_ghosts(const DevInst* inst, int slot, int buf) {
@@ -751,7 +796,7 @@ template <typename T, int DIM, bool EXACT>
 __global__ void k_constrain(const DevInst* inst, int slot, int buf) {
     const DevInst& I = inst[slot];
     TileK<T> K;
-    makeTileK<T>(K, I, 0., 0, 0);
+    makeTileK<T>(K, I, nullptr, nullptr, 0, 0);
     T* base = reinterpret_cast<T*>(I.buf[buf]);
     long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
@@ -769,7 +814,7 @@ template <typename T, int DIM, bool EXACT>
 __global__ void k_calc_dt(const DevInst* inst, DevCtl* ctl, int slot, int buf) {
     const DevInst& I = inst[slot];
     TileK<T> K;
-    makeTileK<T>(K, I, 0., 0, 0);
+    makeTileK<T>(K, I, nullptr, nullptr, 0, 0);
     const T* base = reinterpret_cast<const T*>(I.buf[buf]);
     long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
     double m = __longlong_as_double((long long)kInfBits);

@@ -29,7 +29,7 @@ using namespace fz;
 
 namespace fz {
 
-__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates) {
+__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates, BetaTable bt) {
     int const s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nslots) return;
     DevCtl& c = ctl[s];
@@ -54,15 +54,17 @@ __global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin,
         if (I.stop_on_error || !(dt == dt)) { c.active = 0; c.done = 1; return; }
     }
     c.dt = dt;
+    fillStepCoefs(c, I, bt, dt);
     c.stepping = 1;
 }
 
 // Explicit-dt step of one slot (SolverBase:step(dt): t is not advanced).
-__global__ void k_set_dt(DevCtl* ctl, int slot, double dt, int on, int rotates) {
+__global__ void k_set_dt(DevCtl* ctl, const DevInst* inst, int slot, double dt, int on, int rotates, BetaTable bt) {
     DevCtl& c = ctl[slot];
     if (on) {
         c.dtmin[c.par ^ 1] = kInfBits;
         c.dt = dt;
+        fillStepCoefs(c, inst[slot], bt, dt);
         c.stepping = 1;
     } else {
         c.stepping = 0;
@@ -73,7 +75,7 @@ __global__ void k_set_dt(DevCtl* ctl, int slot, double dt, int on, int rotates) 
 
 // For timing a stage in isolation: mark live slots as stepping with their
 // current CFL dt, without touching t, steps or the dt parity.
-__global__ void k_tune_mode(DevCtl* ctl, const DevInst* inst, int nslots, int on) {
+__global__ void k_tune_mode(DevCtl* ctl, const DevInst* inst, int nslots, int on, BetaTable bt) {
     int const s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nslots) return;
     DevCtl& c = ctl[s];
@@ -82,6 +84,7 @@ __global__ void k_tune_mode(DevCtl* ctl, const DevInst* inst, int nslots, int on
     const DevInst& I = inst[s];
     double const dt = I.fixed_dt > 0 ? I.fixed_dt : I.cfl * __longlong_as_double((long long)c.dtmin[c.par]);
     c.dt = isfinite(dt) && dt > 0 ? dt : 0.;
+    fillStepCoefs(c, I, bt, c.dt);
     c.stepping = 1;
 }
 
@@ -150,6 +153,7 @@ struct FusedSet {
     IntegratorPlan plan[1];        // stages from state buffer 0
     bool rotates = false;          // the plan leaves the state in plan.result_buf (per-slot DevCtl::rot)
     int rot_buf = 0;
+    BetaTable betas;               // beta coefficients of the plan, for the per-step coefficients
     int esize = 4;
     int max_slots = 0;
     cudaStream_t stream = nullptr;
@@ -225,6 +229,12 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
     f->plan[0] = make_plan(sch.integrator);
     f->rotates = f->plan[0].result_buf != 0;
     f->rot_buf = f->rotates ? f->plan[0].result_buf : 0;
+    std::memset(&f->betas, 0, sizeof(f->betas));
+    for (int st = 0; st < f->plan[0].n_stages; ++st) {
+        const StagePlan& S = f->plan[0].stage[st];
+        for (int m = 0; m < S.n_beta; ++m) f->betas.b[st][m] = S.beta[m].coef;
+        f->betas.b[st][4] = S.beta_cur;
+    }
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&f->num_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -463,6 +473,15 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     I.t_end = t_end;
     I.max_steps = max_steps;
     I.stop_on_error = stop_on_error;
+    I.f_gamma = (float)d.gamma;
+    I.f_g1 = (float)(d.gamma - 1.);
+    I.f_rhoMin = (float)d.rho_min;
+    I.f_PMin = (float)d.p_min;
+    I.f_invg1 = (float)(1. / (d.gamma - 1.));
+    for (int k = 0; k < 3; ++k) {
+        I.f_area[k] = (float)I.area[k];
+        I.f_gdx[k] = (float)I.grid_dx[k];
+    }
     char* p = (char*)S.mem;
     for (int b = 0; b < nb; ++b, p += planeBytes * 5) I.buf[b] = p;
     for (int b = 0; b < nd; ++b, p += planeBytes * 5) I.dbuf[b] = p;
@@ -541,12 +560,17 @@ static int rebuild_items(FusedSet* f) {
     return HC_OK;
 }
 
-static void fill_stage(StageDev& sd, const StagePlan& sp) {
+static void fill_stage(StageDev& sd, const StagePlan& sp, int stage) {
     std::memset(&sd, 0, sizeof(sd));
+    sd.stage = stage;
     sd.in_buf = sp.in_buf;
     sd.out_buf = sp.out_buf;
     sd.n_alpha = sp.n_alpha;
-    for (int k = 0; k < sp.n_alpha; ++k) { sd.alpha_buf[k] = sp.alpha[k].buf; sd.alpha[k] = sp.alpha[k].coef; }
+    for (int k = 0; k < sp.n_alpha; ++k) {
+        sd.alpha_buf[k] = sp.alpha[k].buf;
+        sd.alpha[k] = sp.alpha[k].coef;
+        sd.alpha_f[k] = (float)sp.alpha[k].coef;
+    }
     sd.n_beta = sp.n_beta;
     for (int k = 0; k < sp.n_beta; ++k) { sd.beta_buf[k] = sp.beta[k].buf; sd.beta[k] = sp.beta[k].coef; }
     sd.beta_cur = sp.beta_cur;
@@ -568,7 +592,7 @@ static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
             a.nitems = f->d_nitems + d;
             a.err = f->d_err;
             a.rot_buf = f->rot_buf;
-            fill_stage(a.st, P.stage[s]);
+            fill_stage(a.st, P.stage[s], P.stage[s].index);
             f->launcher[d]->launch(a, f->sch.slope_limiter, f->sch.flux_limiter, f->grid[d], f->stream);
         }
     }
@@ -578,7 +602,7 @@ static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
 
 static int launch_step(FusedSet* f, int dims_mask) {
     unsigned const g = (unsigned)((f->max_slots + 127) / 128);
-    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates, f->betas);
     return launch_stages(f, f->plan[0], dims_mask);
 }
 
@@ -604,7 +628,7 @@ int fused_steps(FusedSet* f, int steps) {
     if (!f->graph_valid) HC_CHECK(capture_graph(f));
     for (int k = 0; k < steps; ++k) HC_CUDA(cudaGraphLaunch(f->graph, f->stream));
     unsigned const g = (unsigned)((f->max_slots + 127) / 128);
-    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas);
     HC_CUDA(cudaGetLastError());
     return HC_OK;
 }
@@ -620,7 +644,7 @@ int fused_steps_timed(FusedSet* f, int steps, double* stage_ms, int n_stage_ms, 
     HC_CUDA(cudaEventRecord(ev[k++], f->stream));
     unsigned const g = (unsigned)((f->max_slots + 127) / 128);
     for (int s = 0; s < steps; ++s) {
-        fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates);
+        fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates, f->betas);
         for (int st = 0; st < P.n_stages; ++st) {
             IntegratorPlan one;
             std::memset(&one, 0, sizeof(one));
@@ -631,7 +655,7 @@ int fused_steps_timed(FusedSet* f, int steps, double* stage_ms, int n_stage_ms, 
             HC_CUDA(cudaEventRecord(ev[k++], f->stream));
         }
     }
-    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas);
     HC_CUDA(cudaEventRecord(ev[k++], f->stream));
     HC_CUDA(cudaEventSynchronize(ev[k - 1]));
     size_t j = 1;
@@ -652,9 +676,9 @@ int fused_step_dt(FusedSet* f, int slot, double dt) {
     HC_CHECK(rebuild_items(f));
     const Slot& S = f->slots[slot];
     if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
-    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, slot, dt, 1, f->rotates);
+    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 1, f->rotates, f->betas);
     HC_CHECK(launch_stages(f, f->plan[0], 1 << (S.dim - 1)));
-    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, slot, dt, 0, f->rotates);
+    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 0, f->rotates, f->betas);
     HC_CUDA(cudaGetLastError());
     return HC_OK;
 }
@@ -839,7 +863,7 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
             f->items_dirty = true;
             HC_CHECK(rebuild_items(f));
             unsigned const g = (unsigned)((f->max_slots + 127) / 128);
-            fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1);
+            fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->betas);
             StagePlan sp = f->plan[0].stage[0];
             sp.last = 0;   // no dt atomics while timing
             IntegratorPlan one;
@@ -859,7 +883,7 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
             cudaEventElapsedTime(&ms, e0, e1);
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
-            fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0);
+            fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->betas);
             HC_CUDA(cudaStreamSynchronize(f->stream));
             log << "# " << key << " variant " << v << " tile " << f->launcher[dim - 1]->tx << "x" << f->launcher[dim - 1]->ty
                 << "x" << f->launcher[dim - 1]->tz << " threads " << f->launcher[dim - 1]->nthreads << " ms/stage " << ms / reps << "\n";

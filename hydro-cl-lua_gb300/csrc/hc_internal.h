@@ -52,6 +52,7 @@ const RKTable& rk_table(int integrator);
 // The stage plan turns a table into fused stage launches with buffer reuse.
 struct StageTerm { int buf; double coef; };
 struct StagePlan {
+    int index;                    // stage number within the step (0-based)
     int in_buf;                   // u^(i-1), read with halo
     int out_buf;                  // u^(i)
     int n_alpha;                  // alpha terms, k ascending

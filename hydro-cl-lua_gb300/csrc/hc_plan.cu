@@ -69,6 +69,7 @@ IntegratorPlan make_plan(int integrator) {
 
     for (int s = 1; s <= order; ++s) {
         StagePlan& S = P.stage[s - 1];
+        S.index = s - 1;
         S.in_buf = stateBuf[s];
         S.n_alpha = 0;
         for (int k = 1; k <= s; ++k)

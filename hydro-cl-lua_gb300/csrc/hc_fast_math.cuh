@@ -29,6 +29,7 @@ namespace fast {
 
 template <typename T> struct M;
 template <> struct M<float> {
+    static __device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
     static __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
     static __device__ __forceinline__ bool finite_(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
     static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.f, x); }
@@ -37,6 +38,7 @@ template <> struct M<float> {
     static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
 };
 template <> struct M<double> {
+    static __device__ __forceinline__ double rsqrt_(double x) { return 1. / sqrt(x); }
     static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
     static __device__ __forceinline__ bool finite_(double x) { return isfinite(x); }
     static __device__ __forceinline__ double rcp(double x) { return 1. / x; }
@@ -126,21 +128,22 @@ __device__ __forceinline__ void eigen(EigF<T>& e, const Eos<T>& s, const C5<T>& 
         e.hT = (P + Uo.u[4]) * inv;
         e.Cs = P <= s.PMin ? T(0) : (Uo.u[0] < s.rhoMin ? M<T>::inf() : M<T>::sqrt_(s.gamma * P * inv));
     } else {
-        T invL, PL, invR, PR;
-        primOf(UL, s, invL, PL);
-        primOf(UR, s, invR, PR);
-        T const sL = M<T>::sqrt_(UL.u[0]);
-        T const sR = M<T>::sqrt_(UR.u[0]);
-        T const hTL = (PL + UL.u[4]) * invL;
-        T const hTR = (PR + UR.u[4]) * invR;
+        // one reciprocal square root per side gives sqrt(rho) = rho rs,
+        // 1/rho = rs^2, and the Roe weights: sqrt(rho) v = m rs,
+        // sqrt(rho) hTotal = (P + ETotal) rs
+        T const rsL = M<T>::rsqrt_(UL.u[0]), rsR = M<T>::rsqrt_(UR.u[0]);
+        T const invL = rsL * rsL, invR = rsR * rsR;
+        T const sL = UL.u[0] * rsL, sR = UR.u[0] * rsR;
+        T const m2L = UL.u[1] * UL.u[1] + UL.u[2] * UL.u[2] + UL.u[3] * UL.u[3];
+        T const m2R = UR.u[1] * UR.u[1] + UR.u[2] * UR.u[2] + UR.u[3] * UR.u[3];
+        T const PL = UL.u[0] < s.rhoMin ? T(0) : s.g1 * (UL.u[4] - T(.5) * m2L * invL);
+        T const PR = UR.u[0] < s.rhoMin ? T(0) : s.g1 * (UR.u[4] - T(.5) * m2R * invR);
         T const invDen = M<T>::rcp(sL + sR);
-        // sqrt(rhoL) * v_L = m_L / sqrt(rhoL)
-        T const aL = sL * invDen * invL, aR = sR * invDen * invR;
         rho = sL * sR;
-        e.vn = UL.u[1] * aL + UR.u[1] * aR;
-        e.vt1 = UL.u[2] * aL + UR.u[2] * aR;
-        e.vt2 = UL.u[3] * aL + UR.u[3] * aR;
-        T const hT = invDen * (sL * hTL + sR * hTR);
+        e.vn = (UL.u[1] * rsL + UR.u[1] * rsR) * invDen;
+        e.vt1 = (UL.u[2] * rsL + UR.u[2] * rsR) * invDen;
+        e.vt2 = (UL.u[3] * rsL + UR.u[3] * rsR) * invDen;
+        T const hT = ((PL + UL.u[4]) * rsL + (PR + UR.u[4]) * rsR) * invDen;
         e.vSq = e.vn * e.vn + e.vt1 * e.vt1 + e.vt2 * e.vt2;
         T const eKin = T(.5) * e.vSq;
         T const h = hT - eKin;
@@ -253,9 +256,7 @@ __device__ __forceinline__ void roeSplit(T* F, const Eos<T>& s, const C5<T>& UL,
 
 // "plm cons" slope of one component: returns sigma.
 template <typename T>
-__device__ __forceinline__ T plmSigma(T um, T u0, T up, int lim) {
-    T const dUR = up - u0;
-    T const dUL = u0 - um;
+__device__ __forceinline__ T plmSigmaD(T dUL, T dUR, int lim) {
     T const dUC = T(.5) * (dUR - dUL);
     bool const pos = dUC >= T(0);
     T const num = pos ? dUL : dUR;
@@ -276,9 +277,7 @@ __device__ __forceinline__ T plmSigma(T um, T u0, T up, int lim) {
 // The table's van Leer keeps the general path: its 0/0 at r = -1 is behaviour
 // the reference has.
 template <typename T, int LIMC>
-__device__ __forceinline__ T plmHalfSlope(T um, T u0, T up, int limRT) {
-    T const dUR = up - u0;
-    T const dUL = u0 - um;
+__device__ __forceinline__ T plmHalfSlopeD(T dUL, T dUR, int limRT) {
     if constexpr (LIMC == 8 || LIMC == 17 || LIMC == 18 || LIMC == 20) {
         T const prod = dUL * dUR;
         T h;
@@ -297,7 +296,7 @@ __device__ __forceinline__ T plmHalfSlope(T um, T u0, T up, int limRT) {
         }
         return prod > T(0) ? h : T(0);
     } else {
-        return T(.5) * plmSigma<T>(um, u0, up, LIMC >= 0 ? LIMC : limRT);
+        return T(.5) * plmSigmaD<T>(dUL, dUR, LIMC >= 0 ? LIMC : limRT);
     }
 }
 

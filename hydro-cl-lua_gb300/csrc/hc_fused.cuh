@@ -332,6 +332,7 @@ __device__ __forceinline__ void scatterGhosts(const DevInst& I, T* base, int gx,
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         int const c = g[d], N = I.n[d];
+        if (c >= 2 && c < N - 2) continue;   // no boundary copies this cell
         int tgt[4];
         bool neg[4];
         int nt = 0;
@@ -471,16 +472,21 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
         };
         if constexpr (PLM) {
             C5 Um, U0, Up, prevR, fL, fR;
+            T dL[5];     // U0 - Um, carried from the previous cell's right difference
             load(-2, Um);
             load(-1, U0);
+#pragma unroll
+            for (int j = 0; j < 5; ++j) dL[j] = U0.u[j] - Um.u[j];
 #pragma unroll (UNR == 0 ? L + 2 : UNR)
             for (int k = -1; k <= L; ++k) {
                 load(k + 1, Up);
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
-                    T const sg = fast::plmHalfSlope<T, SLOPE>(Um.u[j], U0.u[j], Up.u[j], slopeLim);
+                    T const dR = Up.u[j] - U0.u[j];
+                    T const sg = fast::plmHalfSlopeD<T, SLOPE>(dL[j], dR, slopeLim);
                     fL.u[j] = U0.u[j] - sg;
                     fR.u[j] = U0.u[j] + sg;
+                    dL[j] = dR;
                 }
                 if (k >= 0) {
                     T Fr[5];
@@ -740,10 +746,9 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                 }
                 constrainCell<T, EXACT>(u, K);
 #pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    out[f * I.plane + idx] = u[f];
-                    bad |= !fast::M<T>::finite_(u[f]);
-                }
+                for (int f = 0; f < 5; ++f) out[f * I.plane + idx] = u[f];
+                // after constrainU a non-finite momentum shows in ETotal
+                bad |= !fast::M<T>::finite_(u[0] + u[4]);
                 scatterGhosts<T, DIM>(I, out, g[0], g[1], g[2], u);
                 if (dstore) {
 #pragma unroll

@@ -712,11 +712,14 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
                     } else {
                         src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m - st.n_alpha]]);
                     }
+                    int const gA = AX == 0 ? gx0 : (AX == 1 ? gy0 : gz0);
+                    int const nAx = AX == 0 ? nx : (AX == 1 ? ny : nz);
 #pragma unroll
                     for (int f = 0; f < 5; ++f)
 #pragma unroll
                         for (int k = 0; k < L; ++k)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(src + f * I.plane + idx0 + k * stepA));
+                            if (gA + k < nAx)   // interior cells only: every address lies inside the plane
+                                asm volatile("prefetch.global.L1 [%0];" ::"l"(src + f * I.plane + idx0 + k * stepA));
                 }
             }
             sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K,

@@ -697,31 +697,6 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
             if (gx0 >= nx || gy0 >= ny || gz0 >= nz) continue;
             int const base = ((c0[2] + (DIM > 2 ? 2 : 0)) * G::BY + (c0[1] + (DIM > 1 ? 2 : 0))) * G::BX + (c0[0] + 2);
             T* Dl = D + (c0[2] * TY + c0[1]) * G::DPX + c0[0];
-            {
-                // the epilogue's pointwise reads of other states and stored
-                // derivatives: start them now, they land in L1 during the sweep
-                int gg[3] = {gx0, gy0, gz0};
-                long long const idx0 = padIndex<DIM>(I, gg[0], gg[1], gg[2]);
-                long long const stepA = AX == 0 ? 1 : (AX == 1 ? (long long)I.px : (long long)I.px * I.py);
-                for (int m = 0; m < st.n_alpha + st.n_beta; ++m) {
-                    const T* src;
-                    if (m < st.n_alpha) {
-                        int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
-                        if (b == inBuf) continue;
-                        src = reinterpret_cast<const T*>(I.buf[b]);
-                    } else {
-                        src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m - st.n_alpha]]);
-                    }
-                    int const gA = AX == 0 ? gx0 : (AX == 1 ? gy0 : gz0);
-                    int const nAx = AX == 0 ? nx : (AX == 1 ? ny : nz);
-#pragma unroll
-                    for (int f = 0; f < 5; ++f)
-#pragma unroll
-                        for (int k = 0; k < L; ++k)
-                            if (gA + k < nAx)   // interior cells only: every address lies inside the plane
-                                asm volatile("prefetch.global.L1 [%0];" ::"l"(src + f * I.plane + idx0 + k * stepA));
-                }
-            }
             sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K,
                 [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll

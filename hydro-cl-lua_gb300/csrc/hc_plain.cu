@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstring>
 #include <algorithm>
+#include <mutex>
 
 namespace hc {
 
@@ -560,3 +561,106 @@ int plain_conservation(PlainSolver* s, double sums[5]) {
 }
 
 }  // namespace hc
+
+// ---------------------------------------------------------------------------
+// calcDT without allocation
+//
+// For callers that cannot allocate device memory at the moment they need a
+// time step: code that is recording a CUDA graph (cudaMalloc is not a stream
+// operation and is refused during stream capture), code that runs under an
+// external memory manager that owns every byte of the device, or a real-time
+// loop that cannot afford the implicit device synchronisation of cudaMalloc.
+// They pass the state and the output in memory they already own; the
+// per-block minima of the reduction live in this fixed array inside the
+// library instead of in a scratch buffer.
+// ---------------------------------------------------------------------------
+
+namespace hc {
+namespace {
+
+constexpr long long kNoAllocBlocks = HC_NOALLOC_MAX_CELLS / kThreads;
+
+// Block minima of k_calcDT.  Every device that loads the library holds this
+// array (512 KiB) until the process exits.  All calls share it: each call
+// writes entries [0, blocks) before reading them, so nothing has to start at
+// zero, but two calls whose kernels overlap on the GPU race on it.
+static __device__ __align__(256) double g_noalloc_partial[kNoAllocBlocks];
+
+// cfl * min over the block minima (or the fixed dt), written to device memory
+__global__ void k_minReduceScaled(const double* in, long long n, double cfl, double* out) {
+    double v = INFINITY;
+    for (long long k = threadIdx.x; k < n; k += blockDim.x) v = fmin(v, in[k]);
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __shared__ double warpMin[32];
+    if ((threadIdx.x & 31) == 0) warpMin[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < blockDim.x / 32 ? warpMin[threadIdx.x] : INFINITY;
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) *out = cfl * v;
+    }
+}
+
+__global__ void k_writeScalar(double v, double* out) { *out = v; }
+
+// Device address of g_noalloc_partial per device, looked up once per device
+// (with that device current) on its first call.
+constexpr int kMaxDevices = 64;
+double* g_noalloc_ptr[kMaxDevices] = {nullptr};
+std::mutex g_noalloc_mutex;
+
+int noalloc_scratch(double** out) {
+    int dev = 0;
+    HC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(HC_ERR_INVALID, "device index beyond the supported range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partial);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_partial)");
+        g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return HC_OK;
+}
+
+}  // namespace
+
+}  // namespace hc
+
+extern "C" int hc_calc_dt_noalloc(const hc_solver_desc* d, const double* state, double* dt_out, void* stream) {
+    using namespace hc;
+    if (!d || !state || !dt_out) return fail(HC_ERR_INVALID, "NULL argument");
+    if (d->dim < 1 || d->dim > 3) return fail(HC_ERR_INVALID, "dim must be 1, 2 or 3");
+    PlainParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.dim = d->dim;
+    for (int k = 0; k < 3; ++k) {
+        int const n = k < d->dim ? d->n[k] : 1;
+        if (n < 1) return fail(HC_ERR_INVALID, "gridSize must be positive");
+        p.gs[k] = k < d->dim ? n + 2 * kGhost : 1;
+        p.grid_dx[k] = (d->maxs[k] - d->mins[k]) / (double)n;
+    }
+    p.stepsize[0] = 1;
+    p.stepsize[1] = p.gs[0];
+    p.stepsize[2] = p.gs[0] * p.gs[1];
+    p.numCells = (long long)p.gs[0] * p.gs[1] * p.gs[2];
+    if (p.numCells > HC_NOALLOC_MAX_CELLS)
+        return fail(HC_ERR_INVALID, "hc_calc_dt_noalloc: the grid (ghosts included) has more than HC_NOALLOC_MAX_CELLS cells");
+    p.gamma = d->gamma;
+    p.rhoMin = d->rho_min;
+    p.PMin = d->p_min;
+    cudaStream_t const s = static_cast<cudaStream_t>(stream);
+    if (d->fixed_dt > 0) {
+        k_writeScalar<<<1, 1, 0, s>>>(d->fixed_dt, dt_out);
+        HC_CUDA(cudaGetLastError());
+        return HC_OK;
+    }
+    double* scratch = nullptr;
+    HC_CHECK(noalloc_scratch(&scratch));
+    long long const blocks = (p.numCells + kThreads - 1) / kThreads;
+    k_calcDT<<<(unsigned)blocks, kThreads, 0, s>>>(p, reinterpret_cast<const Cons*>(state), scratch);
+    k_minReduceScaled<<<1, 1024, 0, s>>>(scratch, blocks, d->cfl, dt_out);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}

@@ -126,6 +126,7 @@ PROTOTYPES = {
     "hc_batch_stats_get": (_ip, [_vp, ctypes.POINTER(BatchStats)]),
     "hc_batch_conservation": (_ip, [_vp, _ip, _dp]),
     "hc_batch_autotune": (_ip, [_vp, ctypes.c_char_p]),
+    "hc_calc_dt_noalloc": (_ip, [ctypes.POINTER(SolverDesc), _vp, _vp, _vp]),
 }
 
 _lib = None

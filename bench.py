@@ -45,6 +45,7 @@ METRIC = "cell-updates/s (FP32 batched)"
 UNIT = "cell-updates/s"
 COUNT = 512
 E2E_STEPS = 200          # the configuration's 200 steps per instance
+STATUS_BYTES_PER_SLOT = 64   # per-slot status head read back after every update
 SCHEME = dict(usePLM="plm cons", slopeLimiter="van Leer (abs)", integrator="Runge-Kutta 2")
 BYTES_PER_VALUE = 4
 FIELDS = 5
@@ -238,11 +239,21 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--count", type=int, default=COUNT,
                     help="instances (the configuration has 512; fewer only for profiling a small case)")
+    ap.add_argument("--workload", default="c4", choices=["c4", "c1", "c2", "c3", "c5"],
+                    help="c4: the batched quadrants (the headline); c1 Sod; c2 Kelvin-Helmholtz 1024^2; "
+                         "c3 blast 256^3; c5 serving")
+    ap.add_argument("--size", type=int, default=0, help="c2 / c3: grid side (default: the configuration's)")
+    ap.add_argument("--requests", type=int, default=1000,
+                    help="c5: requests in the stream (the configuration has 20000)")
+    ap.add_argument("--host-states", action="store_true",
+                    help="c5: build initial states on the host and upload them (default: on the device)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "c4":
+        return {"c1": run_c1, "c2": run_c2, "c3": run_c3, "c5": run_c5}[args.workload](args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
@@ -342,21 +353,24 @@ def e2e_run(hc, ctx, work, inputs, cells):
         b = hc.Batch(ctx, precision="f32", max_slots=len(work), **SCHEME)
         for k, ((a, _), v) in enumerate(zip(work, views)):
             b.admit(a, v, t_end=math.inf, max_steps=E2E_STEPS, tag=k, layout="soa5_f32")
+        t_admit = time.perf_counter()
         steps = 0
         while b.step(1) > 0:
             steps += 1
+        t_step = time.perf_counter()
         got = 0
         for ev in b.poll():
-            views[ev["tag"]][...] = b.fetch(ev["slot"], "soa5_f32")
+            b.fetch(ev["slot"], "soa5_f32", out=views[ev["tag"]])
             got += 1
         t1 = time.perf_counter()
         b.close()
     finally:
         L.hc_host_free(ptr)
-    ctl_bytes = 48 * len(work)
+    ctl_bytes = STATUS_BYTES_PER_SLOT * len(work)
     return {"value": cells * E2E_STEPS / (t1 - t0), "unit": UNIT,
             "h2d_bytes_per_step": nbytes / E2E_STEPS, "d2h_bytes_per_step": nbytes / E2E_STEPS + ctl_bytes,
             "steps": E2E_STEPS, "instances_fetched": got, "seconds": t1 - t0,
+            "seconds_admit": t_admit - t0, "seconds_steps": t_step - t_admit, "seconds_fetch": t1 - t_step,
             "note": "whole job per call: admission (uploads), 200 updates with a per-update status read, result fetch"}
 
 
@@ -389,6 +403,348 @@ def fp64_run(hc, ctx, work):
     b.close()
     return {"plain_value": plain, "plain_sample": "%d grids x 3 updates" % len(sample),
             "fused_batched_value": fused, "unit": UNIT}
+
+
+# ---------------------------------------------------------------------------
+# The other configurations: one JSON line each (--workload c1 | c2 | c3 | c5)
+# ---------------------------------------------------------------------------
+
+def conf_sod(n=256):
+    """1D Sod, x in [-1, 1], gamma 1.4, freeflow, Roe + superbee flux limiter, forward Euler, CFL .5."""
+    return dict(dim=1, gridSize=[n], mins=[-1, -1, -1], maxs=[1, 1, 1], boundary="freeflow",
+                fluxLimiter="superbee", integrator="forward Euler", cfl=.5, eqnArgs={"heatCapacityRatio": 1.4})
+
+
+def conf_kh(n=1024):
+    """2D Kelvin-Helmholtz on [-.5, .5]^2, periodic, plm cons + MC, Roe, RK3-TVD, CFL .4, gamma 1.4."""
+    return dict(dim=2, gridSize=[n, n], mins=[-.5, -.5, -1], maxs=[.5, .5, 1], boundary="periodic",
+                usePLM="plm cons", slopeLimiter="monotized central", integrator="Runge-Kutta 3, TVD",
+                cfl=.4, eqnArgs={"heatCapacityRatio": 1.4})
+
+
+def conf_blast(n=256):
+    """3D blast on [-1, 1]^3, freeflow, plm cons + minmod, Roe, RK2, CFL .3, gamma 5/3."""
+    return dict(dim=3, gridSize=[n, n, n], mins=[-1, -1, -1], maxs=[1, 1, 1], boundary="freeflow",
+                usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2",
+                cfl=.3, eqnArgs={"heatCapacityRatio": 5. / 3.})
+
+
+def _cells(args):
+    return int(np.prod(args["gridSize"]))
+
+
+def _scheme(args):
+    return {k: args[k] for k in ("usePLM", "slopeLimiter", "fluxLimiter", "integrator") if k in args}
+
+
+def l1_density(a, b):
+    """Mean |rho_a - rho_b| over the interior cells (AoS-6 states; equal cell volumes)."""
+    return float(np.mean(np.abs(a[:, 0] - b[:, 0])))
+
+
+def batch_solve(hc, ctx, args, cons, precision, t_end=math.inf, max_steps=0, chunk=16, init=None):
+    """One solve through the batch API, device-timed stage by stage.  Runs
+    until the instance reports done (t >= t_end or max_steps updates).
+    Returns the final AoS-6 interior state, updates done, device ms and the
+    Kahan FP64 sums of the conserved fields before and after."""
+    b = hc.Batch(ctx, precision=precision, max_slots=1, **_scheme(args))
+    try:
+        if init is not None:
+            slot = b.admit_init(args, init[0], t_end=t_end, max_steps=max_steps, tag=0, **init[1])
+        else:
+            slot = b.admit(args, cons, t_end=t_end, max_steps=max_steps, tag=0)
+        sums0 = b.conservation(slot)
+        total_ms = 0.0
+        ev = []
+        while not ev:
+            n = chunk if not max_steps else max(1, min(chunk, max_steps))
+            _, ms = b.step_timed(n)
+            total_ms += ms
+            ev = b.poll()
+        state = b.fetch(slot, "aos6")
+        sums1 = b.conservation(slot)
+        return dict(state=state, steps=ev[0]["steps"], t=ev[0]["t"], ms=total_ms, status=ev[0]["status"],
+                    sums0=sums0, sums1=sums1)
+    finally:
+        b.close()
+
+
+def warm(hc, ctx, args, cons, precision):
+    """Loads the kernels of a form (lazy module loading) outside any timed region."""
+    batch_solve(hc, ctx, args, cons, precision, max_steps=2, chunk=2)
+
+
+def plain_rate(hc, ctx, args, cons, updates):
+    """The plain FP64 form (kernel per reference kernel, host dt read per update)."""
+    s = hc.Solver(ctx, precision="f64 plain", **args)
+    try:
+        s.resetState(cons)
+        s.update()
+        t0 = time.perf_counter()
+        for _ in range(updates):
+            s.update()
+        dt = time.perf_counter() - t0
+    finally:
+        s.close()
+    return _cells(args) * updates / dt
+
+
+def oracle_rate(hc, args, cons, updates):
+    """The oracle (the reference's kernels restated in C++, OpenMP on every host core)."""
+    import oracle
+    oracle.build()
+    o = oracle.OracleSolver(args)
+    o.reset_state(cons)
+    o.update()
+    t0 = time.perf_counter()
+    for _ in range(updates):
+        o.update()
+    dt = time.perf_counter() - t0
+    return {"value": _cells(args) * updates / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": "%d update(s) of the full grid after one untimed update" % updates}
+
+
+def fp64_first_update_vs_oracle(hc, ctx, args, cons):
+    """Max |difference| between the fused FP64 form and the oracle after one
+    update of the full-size grid (the parity tests require 0)."""
+    import oracle
+    oracle.build()
+    o = oracle.OracleSolver(args)
+    o.reset_state(cons)
+    o.update()
+    r = batch_solve(hc, ctx, args, cons, "f64", max_steps=1, chunk=1)
+    return float(np.max(np.abs(r["state"] - o.get_interior())))
+
+
+def drift(r):
+    s0, s1 = r["sums0"], r["sums1"]
+    return {"mass": float((s1[0] - s0[0]) / s0[0]), "energy": float((s1[4] - s0[4]) / s0[4])}
+
+
+def config_line(name, metric, value, extra):
+    out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "data": "synthetic"}
+    out.update(extra)
+    out["config"] = dict(out.get("config", {}), workload=name)
+    print(json.dumps(out))
+    return 0
+
+
+def run_c1(args):
+    """1D Sod, 256 cells, to t = 0.2: the plain FP64 form's parity case."""
+    import hydrocuda as hc
+    import oracle
+    from sod_exact import sod_exact
+    ctx = hc.Context(0)
+    a = conf_sod()
+    U0 = hc.sod_state(a)
+    oracle.build()
+    o = oracle.OracleSolver(a)
+    o.reset_state(U0)
+    t0 = time.perf_counter()
+    o.run_until(0.2)
+    t_cpu = time.perf_counter() - t0
+    ref = o.get_interior()
+    res = {}
+    for prec in ("f64 plain", "f64", "f32"):
+        s = hc.Solver(ctx, precision=prec, **a)
+        s.resetState(U0)
+        s.update()          # loads the kernels
+        s.resetState(U0)
+        s.t = 0.0
+        t0 = time.perf_counter()
+        n = s.run_until(0.2)
+        el = time.perf_counter() - t0
+        g = s.getState("aos6")
+        res[prec] = {"seconds": el, "updates": n, "max_abs_diff_vs_oracle": float(np.max(np.abs(g - ref))),
+                     "l1_rho_vs_oracle": l1_density(g, ref)}
+        s.close()
+    x = hc.cell_centers(a)[0]
+    exact = sod_exact(o.t, x, gamma=1.4)[0]
+    plain = res["f64 plain"]
+    return config_line("1D Sod 256, Roe + superbee, forward Euler, CFL .5, t = 0.2", "cell-updates/s (FP64 plain)",
+                       256 * plain["updates"] / plain["seconds"], {
+                           "dtype": "f64", "forms": res,
+                           "l1_rho_oracle_vs_exact_sod": float(np.mean(np.abs(ref[:, 0] - exact))),
+                           "cpu_baseline": {"value": 256 * plain["updates"] / t_cpu, "unit": UNIT,
+                                            "cores": oracle.num_threads(), "kind": "port",
+                                            "sample": "the whole run"},
+                           "note": "launch-bound at this size; this configuration is the parity case"})
+
+
+def run_grid_config(name, a, U0, t_end, max_steps, plain_updates, oracle_updates):
+    import hydrocuda as hc
+    ctx = hc.Context(0)
+    small = dict(a, gridSize=[min(n, 32) for n in a["gridSize"]])
+    U_small = None
+    for prec in ("f32", "f64"):
+        if U_small is None:
+            U_small = initial_for(hc, small)
+        warm(hc, ctx, small, U_small, prec)
+    r32 = batch_solve(hc, ctx, a, U0, "f32", t_end=t_end, max_steps=max_steps)
+    r64 = batch_solve(hc, ctx, a, U0, "f64", t_end=t_end, max_steps=max_steps)
+    cells = _cells(a)
+    v32 = cells * r32["steps"] / (r32["ms"] / 1e3)
+    v64 = cells * r64["steps"] / (r64["ms"] / 1e3)
+    n_stages = {"forward Euler": 1, "Runge-Kutta 2": 2, "Runge-Kutta 3, TVD": 3}[a["integrator"]]
+    arrays = {1: 2, 2: 5, 3: 8}[n_stages]           # state arrays read + written per update
+    gbs = v32 * arrays * FIELDS * BYTES_PER_VALUE / 1e9
+    peaks, peak_kind = measured_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    extra = {
+        "dtype": "f32", "steps": r32["steps"], "t_end_reached": r32["t"],
+        "ms_total": r32["ms"],
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "note": "algorithmic bytes: %d state arrays x 5 fields x 4 B per cell-update" % arrays},
+        "l1_rho_f32_vs_f64": l1_density(r32["state"], r64["state"]),
+        "fp64": {"fused_value": v64, "plain_value": plain_rate(hc, ctx, a, U0, plain_updates),
+                 "plain_sample": "%d updates" % plain_updates,
+                 "fused_first_update_max_abs_diff_vs_oracle": fp64_first_update_vs_oracle(hc, ctx, a, U0)},
+        "drift": {"f32": drift(r32), "f64": drift(r64)},
+        "status": {"f32": r32["status"], "f64": r64["status"]},
+        "cpu_baseline": oracle_rate(hc, a, U0, oracle_updates),
+        "config": {"cells": cells, "l2": "inputs %s than L2 (%.0f MB per state array)" % (
+            "larger" if cells * 20 > 129e6 else "smaller", cells * 20 / 1e6)},
+    }
+    extra["fp64"]["speedup_f32_vs_plain"] = v32 / extra["fp64"]["plain_value"]
+    return config_line(name, "cell-updates/s (FP32 fused)", v32, extra)
+
+
+def initial_for(hc, a):
+    if a["dim"] == 2 and a["boundary"] == "periodic":
+        return hc.kelvin_helmholtz_state(a, seed=2)
+    if a["dim"] == 3:
+        return hc.blast_state(a)
+    return hc.sod_state(a)
+
+
+def run_c2(args):
+    import hydrocuda as hc
+    a = conf_kh(args.size or 1024)
+    return run_grid_config("2D Kelvin-Helmholtz %d^2, plm cons + MC, Roe, RK3-TVD, CFL .4, periodic, 500 steps"
+                           % a["gridSize"][0], a, hc.kelvin_helmholtz_state(a, seed=2), math.inf, 500, 10, 2)
+
+
+def run_c3(args):
+    import hydrocuda as hc
+    a = conf_blast(args.size or 256)
+    return run_grid_config("3D blast %d^3, plm cons + minmod, Roe, RK2, CFL .3, gamma 5/3, freeflow, t = 0.1"
+                           % a["gridSize"][0], a, hc.blast_state(a), 0.1, 0, 3, 1)
+
+
+class StatePrefetch:
+    """Builds request states on worker threads, a bounded number of requests
+    ahead of admission, so the serving loop does not wait on host-side set-up
+    of inputs (which stands in for clients uploading their states).  Time the
+    loop still spends waiting for a state is reported."""
+
+    def __init__(self, reqs, workers=4, ahead=96):
+        from concurrent.futures import ThreadPoolExecutor
+        self.pool = ThreadPoolExecutor(max_workers=workers)
+        self.reqs = reqs
+        self.makers = {r.tag: r.cons for r in reqs}
+        self.futs = {}
+        self.next = 0
+        self.taken = 0
+        self.ahead = ahead
+        self.wait_s = 0.0
+        for r in reqs:
+            r.cons = (lambda tag: lambda: self.get(tag))(r.tag)
+        self._fill()
+
+    def _fill(self):
+        while self.next < len(self.reqs) and self.next < self.taken + self.ahead:
+            tag = self.reqs[self.next].tag
+            self.futs[tag] = self.pool.submit(self.makers.pop(tag))
+            self.next += 1
+
+    def get(self, tag):
+        t0 = time.perf_counter()
+        a = self.futs.pop(tag).result()
+        self.wait_s += time.perf_counter() - t0
+        self.taken += 1
+        self._fill()
+        return a
+
+    def close(self):
+        self.pool.shutdown(wait=True, cancel_futures=True)
+
+
+def run_c5(args):
+    """Serving: a Poisson stream (mean 200 requests/s) of 1D / 2D / 3D solves
+    through the continuous-batching loop, FP32 bulk, 150 GB HBM budget."""
+    import hydrocuda as hc
+    import serve
+    ctx = hc.Context(0)
+    scheme = dict(usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2")
+    budget = 150 * (1 << 30)
+    # load the 1D / 2D / 3D kernels outside the measured run
+    warm_reqs = serve.synthetic_stream(24, rate_hz=1e6, seed=11, scale=0.05)
+    wb = hc.Batch(ctx, precision="f32", max_slots=64, hbm_budget=budget, **scheme)
+    serve.Server(wb, steps_per_tick=4, keep_results=False).run(warm_reqs)
+    wb.close()
+
+    device_init = not args.host_states
+    reqs = serve.synthetic_stream(args.requests, rate_hz=200.0, seed=5, lazy=True, layout="soa5_f32",
+                                  device_init=device_init)
+    # FP64 cross-check sample: the first few requests of each dimension small
+    # enough to solve alone in FP64 within seconds, from their FP64 states
+    limits = {1: (2, 2048), 2: (4, 200), 3: (2, 72)}
+    sample, per = [], {1: 0, 2: 0, 3: 0}
+    for r in reqs:
+        d = r.args["dim"]
+        if per[d] < limits[d][0] and r.args["gridSize"][0] <= limits[d][1]:
+            sample.append(r.tag)
+            per[d] += 1
+    f64_stream = serve.synthetic_stream(args.requests, rate_hz=200.0, seed=5, lazy=True, layout="aos6",
+                                        device_init=True)
+    sample_in = {r.tag: (r.args, r.init, r.t_end) for r in f64_stream if r.tag in set(sample)}
+    pre = StatePrefetch(reqs) if not device_init else None
+    b = hc.Batch(ctx, precision="f32", max_slots=1024, hbm_budget=budget, **scheme)
+    srv = serve.Server(b, steps_per_tick=8, keep_results=set(sample))
+    t0 = time.perf_counter()
+    done = srv.run(reqs)
+    wall = time.perf_counter() - t0
+    if pre:
+        pre.close()
+    b.close()
+    lat = serve.latency_summary(done)
+    value = srv.cell_updates / wall
+    # served FP32 results against the same requests solved alone in FP64
+    l1 = []
+    by_tag = {r.tag: r for r in done}
+    for tag, (a, init, t_end) in sample_in.items():
+        r = by_tag.get(tag)
+        if r is None or r.result is None:
+            continue
+        f64 = batch_solve(hc, ctx, dict(a, **scheme), None, "f64", t_end=t_end, init=init)["state"]
+        l1.append(l1_density(r.result, f64))
+    peaks, peak_kind = measured_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    gbs = value * 5 * FIELDS * BYTES_PER_VALUE / 1e9
+    dims = {1: 0, 2: 0, 3: 0}
+    for r in reqs:
+        dims[r.args["dim"]] += 1
+    return config_line(
+        "serving: Poisson stream, mean 200 req/s, %d requests (40%% 1D N in [512,65536], 45%% 2D N^2 in "
+        "[128^2,1024^2], 15%% 3D N^3 in [64^3,192^3]), t_end ~ U(0.05,0.2), plm cons + minmod, RK2, CFL .3, "
+        "150 GB budget" % len(reqs), "cell-updates/s (FP32 served)", value, {
+            "dtype": "f32", "requests": len(reqs), "finished": len(done), "wall_s": wall,
+            "requests_per_s": len(done) / wall, "latency": lat,
+            "statuses_nonzero": sum(1 for r in done if r.status),
+            "ticks": srv.ticks, "dims": dims,
+            "initial_states": "built on the device at admission (hc_batch_admit_init)" if device_init else
+                              "built on the host by worker threads, uploaded at admission",
+            "host_state_wait_s": pre.wait_s if pre else 0.0,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "note": "algorithmic bytes: RK2, 5 state arrays x 5 fields x 4 B per cell-update"},
+            "l1_rho_f32_vs_f64": {"max": max(l1) if l1 else None, "mean": float(np.mean(l1)) if l1 else None,
+                                  "sample": "%d requests (1D N <= 2048, 2D N <= 200, 3D N <= 72), each solved "
+                                            "alone in FP64 from its FP64 state" % len(l1)},
+            "config": {"arrival_rate_hz": 200.0, "seed": 5, "hbm_budget_bytes": budget, "steps_per_tick": 8,
+                       "note": "the configuration's stream has 20000 requests; --requests sets the count"}})
 
 
 if __name__ == "__main__":

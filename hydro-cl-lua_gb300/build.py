@@ -27,11 +27,13 @@ SOURCES = {
     "hc_api.cu": [],
     "hc_plan.cu": [],
     "hc_plain.cu": EXACT,
+    "hc_init.cu": EXACT,
     "hc_fused_host.cu": [],
     "hc_fused_f32_d1.cu": FAST,
     "hc_fused_f32_d2a.cu": FAST,
     "hc_fused_f32_d2b.cu": FAST,
     "hc_fused_f32_d2c.cu": FAST,
+    "hc_fused_f32_d2d.cu": FAST,
     "hc_fused_f32_d3.cu": FAST,
     "hc_fused_f64_d1.cu": EXACT,
     "hc_fused_f64_d2.cu": EXACT,

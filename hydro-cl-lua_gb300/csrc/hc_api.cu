@@ -1,6 +1,7 @@
 // hc_api.cu -- the extern "C" entry points declared in include/hydrocuda.h.
 #include "hc_internal.h"
 
+#include <atomic>
 #include <cmath>
 #include <climits>
 #include <cstdio>
@@ -28,10 +29,24 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 using namespace hc;
 
+// A context lives until the caller has destroyed it and every solver and
+// batch made on it has been destroyed too (one reference each), so handles
+// may be released in any order.
 struct hc_context {
     int device;
     cudaStream_t stream;
+    std::atomic<int> refs{1};
 };
+
+static void ctx_retain(hc_context* ctx) { ctx->refs.fetch_add(1); }
+
+static void ctx_release(hc_context* ctx) {
+    if (ctx->refs.fetch_sub(1) != 1) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
 
 struct hc_solver {
     hc_context* ctx;
@@ -131,10 +146,7 @@ int hc_context_create(int device, hc_context** out) {
 
 int hc_context_destroy(hc_context* ctx) {
     if (!ctx) return HC_OK;
-    cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    ctx_release(ctx);
     return HC_OK;
 }
 
@@ -151,12 +163,36 @@ int hc_host_free(void* p) {
 
 // ---- solver ---------------------------------------------------------------
 
+static long long full_cells(const hc_solver_desc& d) {
+    long long n = 1;
+    for (int k = 0; k < d.dim; ++k) n *= d.n[k] + 4;
+    return n;
+}
+
+// the interior cells of a ghost-inclusive AoS-6 array (x fastest)
+static void copy_interior(const hc_solver_desc& d, const double* full, double* interior) {
+    int gs[3], n[3];
+    for (int k = 0; k < 3; ++k) {
+        n[k] = k < d.dim ? d.n[k] : 1;
+        gs[k] = k < d.dim ? d.n[k] + 4 : 1;
+    }
+    int const g[3] = {d.dim > 0 ? 2 : 0, d.dim > 1 ? 2 : 0, d.dim > 2 ? 2 : 0};
+    size_t o = 0;
+    for (int k = 0; k < n[2]; ++k)
+        for (int j = 0; j < n[1]; ++j) {
+            size_t const src = ((size_t)(k + g[2]) * gs[1] + (j + g[1])) * gs[0] + g[0];
+            std::memcpy(interior + o * 6, full + src * 6, (size_t)n[0] * 6 * sizeof(double));
+            o += (size_t)n[0];
+        }
+}
+
 int hc_solver_create(hc_context* ctx, const hc_solver_desc* desc, hc_solver** out) {
     if (!ctx || !out) return fail(HC_ERR_INVALID, "NULL argument");
     HC_CHECK(validate_desc(desc));
     HC_CHECK(use_device(ctx));
     hc_solver* s = new hc_solver();
     s->ctx = ctx;
+    ctx_retain(ctx);
     s->d = *desc;
     int r;
     if (desc->precision == HC_F64_PLAIN) {
@@ -180,7 +216,9 @@ int hc_solver_destroy(hc_solver* s) {
     cudaSetDevice(s->ctx->device);
     if (s->plain) plain_destroy(s->plain);
     if (s->fused) fused_destroy(s->fused);
+    hc_context* const ctx = s->ctx;
     delete s;
+    ctx_release(ctx);
     return HC_OK;
 }
 
@@ -201,12 +239,34 @@ int hc_solver_reset_state(hc_solver* s, const void* cons, int layout) {
     return fused_sync(s->fused);
 }
 
+int hc_solver_init_state(hc_solver* s, const hc_init* init) {
+    if (!s || !init) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(s->ctx));
+    HC_CHECK(init_validate(*init, s->d));
+    if (s->plain) {
+        HC_CHECK(plain_init_state(s->plain, *init, s->d));
+        HC_CHECK(plain_boundary(s->plain));
+        HC_CHECK(plain_constrain_u(s->plain));
+        s->t = 0;
+        s->steps = 0;
+        HC_CUDA(cudaStreamSynchronize(s->ctx->stream));
+        return HC_OK;
+    }
+    HC_CHECK(fused_init_state(s->fused, 0, *init));
+    return fused_sync(s->fused);
+}
+
 int hc_solver_set_state(hc_solver* s, const void* cons, int layout, int with_ghosts) {
     if (!s || !cons) return fail(HC_ERR_INVALID, "NULL argument");
     HC_CHECK(use_device(s->ctx));
     if (with_ghosts) {
-        if (!s->plain || layout != HC_LAYOUT_AOS6_F64) return fail(HC_ERR_INVALID, "ghost-inclusive state I/O is AOS6_F64 on the plain form only");
-        return plain_set_full(s->plain, (const double*)cons);
+        if (layout != HC_LAYOUT_AOS6_F64) return fail(HC_ERR_INVALID, "ghost-inclusive state I/O is AOS6_F64");
+        if (s->plain) return plain_set_full(s->plain, (const double*)cons);
+        // the fused forms take the interior; their ghosts follow from the boundary
+        std::vector<double> in((size_t)interior_cells(s->d) * 6);
+        copy_interior(s->d, static_cast<const double*>(cons), in.data());
+        HC_CHECK(fused_set_state(s->fused, 0, in.data(), HC_LAYOUT_AOS6_F64, 0));
+        return fused_sync(s->fused);
     }
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
     if (s->plain) return plain_set_interior(s->plain, cons, layout);
@@ -218,8 +278,23 @@ int hc_solver_get_state(hc_solver* s, void* cons, int layout, int with_ghosts) {
     if (!s || !cons) return fail(HC_ERR_INVALID, "NULL argument");
     HC_CHECK(use_device(s->ctx));
     if (with_ghosts) {
-        if (!s->plain || layout != HC_LAYOUT_AOS6_F64) return fail(HC_ERR_INVALID, "ghost-inclusive state I/O is AOS6_F64 on the plain form only");
-        return plain_get_full(s->plain, (double*)cons);
+        if (layout != HC_LAYOUT_AOS6_F64) return fail(HC_ERR_INVALID, "ghost-inclusive state I/O is AOS6_F64");
+        if (s->plain) return plain_get_full(s->plain, (double*)cons);
+        // the fused forms: the interior, expanded to the reference's UBuf by its boundary rules
+        size_t const nin = (size_t)interior_cells(s->d), nfull = (size_t)full_cells(s->d);
+        void* tmp = nullptr;
+        HC_CUDA(cudaMalloc(&tmp, (nin + nfull) * 6 * sizeof(double)));
+        double* interior = static_cast<double*>(tmp);
+        double* full = interior + nin * 6;
+        int r = fused_get_state_dev(s->fused, 0, interior, HC_LAYOUT_AOS6_F64);
+        if (r == HC_OK) r = plain_expand_full(s->d, interior, HC_LAYOUT_AOS6_F64, full, s->ctx->stream);
+        if (r == HC_OK) {
+            cudaError_t e = cudaMemcpyAsync(cons, full, nfull * 6 * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);
+            if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync");
+        }
+        cudaFree(tmp);
+        return r;
     }
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
     if (s->plain) return plain_get_interior(s->plain, cons, layout);
@@ -379,6 +454,7 @@ int hc_batch_create(hc_context* ctx, const hc_batch_desc* desc, hc_batch** out) 
     b->d = *desc;
     int const r = fused_create(sch, desc->max_slots, ctx->stream, &b->fused);
     if (r != HC_OK) { delete b; return r; }
+    ctx_retain(ctx);
     b->slot_bytes.assign(desc->max_slots, 0);
     b->tags.assign(desc->max_slots, 0);
     b->used.assign(desc->max_slots, 0);
@@ -391,14 +467,17 @@ int hc_batch_destroy(hc_batch* b) {
     if (!b) return HC_OK;
     cudaSetDevice(b->ctx->device);
     fused_destroy(b->fused);
+    hc_context* const ctx = b->ctx;
     delete b;
+    ctx_release(ctx);
     return HC_OK;
 }
 
-int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout,
-                   double t_end, long long max_steps, unsigned long long tag, int* slot) {
-    if (!b || !desc || !cons || !slot) return fail(HC_ERR_INVALID, "NULL argument");
+static int batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout, const hc_init* init,
+                       double t_end, long long max_steps, unsigned long long tag, int* slot) {
+    if (!b || !desc || !(cons || init) || !slot) return fail(HC_ERR_INVALID, "NULL argument");
     HC_CHECK(validate_desc(desc));
+    if (init) HC_CHECK(init_validate(*init, *desc));
     if (desc->recon != b->d.recon || desc->slope_limiter != b->d.slope_limiter || desc->flux_limiter != b->d.flux_limiter ||
         desc->integrator != b->d.integrator)
         return fail(HC_ERR_INVALID, "the instance's scheme differs from the batch's");
@@ -412,7 +491,7 @@ int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, in
     for (int k = 0; k < b->d.max_slots; ++k)
         if (!b->used[k]) { s = k; break; }
     if (s < 0) return fail(HC_ERR_NO_SLOT, "every slot is in use");
-    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps, 1));
+    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps, 1, init));
     b->used[s] = 1;
     b->reported[s] = 0;
     b->tags[s] = tag;
@@ -420,6 +499,18 @@ int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, in
     b->bytes_in_use += bytes;
     *slot = s;
     return HC_OK;
+}
+
+int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout,
+                   double t_end, long long max_steps, unsigned long long tag, int* slot) {
+    if (!cons) return fail(HC_ERR_INVALID, "NULL argument");
+    return batch_admit(b, desc, cons, layout, nullptr, t_end, max_steps, tag, slot);
+}
+
+int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* init,
+                        double t_end, long long max_steps, unsigned long long tag, int* slot) {
+    if (!init) return fail(HC_ERR_INVALID, "NULL argument");
+    return batch_admit(b, desc, nullptr, HC_LAYOUT_AOS6_F64, init, t_end, max_steps, tag, slot);
 }
 
 int hc_batch_step(hc_batch* b, int steps, int* n_active) {

@@ -34,9 +34,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "hc_internal.h"
 #include "hc_ref_math.cuh"
 #include "hc_fast_math.cuh"
+#include "hc_lanes.cuh"
 
 namespace hc {
 namespace fz {
@@ -328,38 +331,46 @@ __device__ __forceinline__ T dtCell(const T* u, const TileK<T>& K, const DevInst
 // not written.
 template <typename T, int DIM>
 __device__ __forceinline__ void scatterGhosts(const DevInst& I, T* base, int gx, int gy, int gz, const T* u) {
-    int g[3] = {gx, gy, gz};
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-        int const c = g[d], N = I.n[d];
+        int const c = d == 0 ? gx : (d == 1 ? gy : gz), N = I.n[d];
         if (c >= 2 && c < N - 2) continue;   // no boundary copies this cell
-        int tgt[4];
-        bool neg[4];
-        int nt = 0;
-        int const lo = I.bc[2 * d], hi = I.bc[2 * d + 1];
-        if (lo == HC_BOUNDARY_PERIODIC && c >= N - 2) { tgt[nt] = c - N; neg[nt++] = false; }
-        if (lo == HC_BOUNDARY_MIRROR && c <= 1) { tgt[nt] = -1 - c; neg[nt++] = true; }
-        if (lo == HC_BOUNDARY_FREEFLOW && c == 0) { tgt[nt] = -1; neg[nt++] = false; tgt[nt] = -2; neg[nt++] = false; }
-        if (hi == HC_BOUNDARY_PERIODIC && c <= 1) { tgt[nt] = N + c; neg[nt++] = false; }
-        if (hi == HC_BOUNDARY_MIRROR && c >= N - 2) { tgt[nt] = N + (N - 1 - c); neg[nt++] = true; }
-        if (hi == HC_BOUNDARY_FREEFLOW && c == N - 1) { tgt[nt] = N; neg[nt++] = false; tgt[nt] = N + 1; neg[nt++] = false; }
-        for (int k = 0; k < nt; ++k) {
-            int h[3] = {gx, gy, gz};
-            h[d] = tgt[k];
-            long long const idx = padIndex<DIM>(I, h[0], h[1], h[2]);
+        // ghost cell at coordinate t along axis d; `neg` negates the normal momentum
+        auto put = [&](int t, bool neg) {
+            long long const idx = padIndex<DIM>(I, d == 0 ? t : gx, d == 1 ? t : gy, d == 2 ? t : gz);
 #pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                T v = u[f];
-                if (neg[k] && f == 1 + d) v = T(-1) * v;
-                base[f * I.plane + idx] = v;
-            }
-        }
+            for (int f = 0; f < 5; ++f) base[f * I.plane + idx] = neg && f == 1 + d ? T(-1) * u[f] : u[f];
+        };
+        int const lo = I.bc[2 * d], hi = I.bc[2 * d + 1];
+        if (lo == HC_BOUNDARY_PERIODIC && c >= N - 2) put(c - N, false);
+        if (lo == HC_BOUNDARY_MIRROR && c <= 1) put(-1 - c, true);
+        if (lo == HC_BOUNDARY_FREEFLOW && c == 0) { put(-1, false); put(-2, false); }
+        if (hi == HC_BOUNDARY_PERIODIC && c <= 1) put(N + c, false);
+        if (hi == HC_BOUNDARY_MIRROR && c >= N - 2) put(N + (N - 1 - c), true);
+        if (hi == HC_BOUNDARY_FREEFLOW && c == N - 1) { put(N, false); put(N + 1, false); }
     }
 }
 
 // ---------------------------------------------------------------------------
 // line sweeps
 // ---------------------------------------------------------------------------
+
+// deriv - (FR * area - FL * area): calcDerivFromFlux's update of one field
+// (fvsolver.cl:37-102).  The exact form keeps the reference's expression.  The
+// fast form evaluates deriv + (FL - FR) * area with explicitly rounded
+// operations: a sweep's left flux is the previous cell's right flux, so
+// unrolled and rolled schedules would otherwise fuse different products into
+// FMAs and round differently; this way every schedule gives the same bits.
+template <typename T, bool EXACT>
+__device__ __forceinline__ T fluxDiff(T deriv, T FL, T FR, T area) {
+    if constexpr (EXACT) {
+        return deriv - (FR * area - FL * area);
+    } else if constexpr (sizeof(T) == 4) {
+        return __fmaf_rn(__fsub_rn(FL, FR), area, deriv);
+    } else {
+        return __fma_rn(__dsub_rn(FL, FR), area, deriv);
+    }
+}
 
 // Box geometry of a tile configuration.
 template <int DIM, int TX, int TY, int TZ>
@@ -549,6 +560,111 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
     }
 }
 
+// Sweeps one segment of L cells along AXIS on nlanes<V>() neighbouring lines
+// at once (fast form, no flux limiter): lane l's line starts at box index
+// base + l * LSTRIDE.  emit(k, FL, FR) receives, for cell k of the segment,
+// the left and right face fluxes of every lane in the global frame.
+template <typename V, int AXIS, int STRIDE, int LSTRIDE, int BOXN, int L, bool PLM, int SLOPE, int UNR, class Emit>
+__device__ __forceinline__ void sweepLanes(const float* box, int base, const lanes::Eos& e, int slopeLim, bool zero,
+                                           Emit&& emit) {
+    using C5 = lanes::C5<V>;
+    constexpr int A1 = 1 + AXIS, A2 = 1 + (AXIS + 1) % 3, A3 = 1 + (AXIS + 2) % 3;
+    constexpr int NL = lanes::nlanes<V>();
+    auto ld = [&](int f, int i) -> V {
+        V v;
+        if constexpr (NL == 1) {
+            v = box[f * BOXN + i];
+        } else if constexpr (LSTRIDE == 1) {
+            v = *reinterpret_cast<const float2*>(box + f * BOXN + i);   // neighbouring columns: one 8-byte load
+        } else {
+            v = make_float2(box[f * BOXN + i], box[f * BOXN + i + LSTRIDE]);
+        }
+        return v;
+    };
+    // loads in the interface frame (rho, m_n, m_t1, m_t2, E)
+    auto load = [&](int k, C5& U) {
+        int const i = base + k * STRIDE;
+        U.u[0] = ld(0, i);
+        U.u[1] = ld(A1, i);
+        U.u[2] = ld(A2, i);
+        U.u[3] = ld(A3, i);
+        U.u[4] = ld(4, i);
+    };
+    V F[5], Fprev[5];
+    auto flux = [&](const C5& UL, const C5& UR) {
+        V Fr[5];
+        lanes::roeSplit<V>(Fr, e, UL, UR);
+        if (zero) for (int j = 0; j < 5; ++j) Fr[j] = lanes::splat<V>(0.f);
+        F[0] = Fr[0];
+        F[A1] = Fr[1];
+        F[A2] = Fr[2];
+        F[A3] = Fr[3];
+        F[4] = Fr[4];
+    };
+    if constexpr (PLM) {
+        C5 Um, U0, Up, prevR, fL, fR;
+        V dL[5];
+        load(-2, Um);
+        load(-1, U0);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) dL[j] = lanes::sub(U0.u[j], Um.u[j]);
+#pragma unroll (UNR == 0 ? L + 2 : UNR)
+        for (int k = -1; k <= L; ++k) {
+            load(k + 1, Up);
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                V const dR = lanes::sub(Up.u[j], U0.u[j]);
+                V const h = lanes::halfSlope<SLOPE>(dL[j], dR, slopeLim);
+                fL.u[j] = lanes::sub(U0.u[j], h);
+                fR.u[j] = lanes::add(U0.u[j], h);
+                dL[j] = dR;
+            }
+            if (k >= 0) {
+                flux(prevR, fL);
+                if (k >= 1) emit(k - 1, Fprev, F);
+#pragma unroll
+                for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
+            }
+            prevR = fR;
+            Um = U0;
+            U0 = Up;
+        }
+    } else {
+        C5 Ua, Ub;
+        load(-1, Ua);
+#pragma unroll (UNR == 0 ? L + 1 : UNR)
+        for (int k = 0; k <= L; ++k) {
+            load(k, Ub);
+            flux(Ua, Ub);
+            if (k >= 1) emit(k - 1, Fprev, F);
+#pragma unroll
+            for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
+            Ua = Ub;
+        }
+    }
+}
+
+__device__ __forceinline__ double laneOf(double v, int) { return v; }
+__device__ __forceinline__ float laneOf(float v, int) { return v; }
+__device__ __forceinline__ float laneOf(float2 v, int k) { return k ? v.y : v.x; }
+
+// One segment sweep: the FP32 fast form without a flux limiter runs the
+// lane-generic arithmetic (LANES lines at once); the exact form and the
+// flux-limited fast form run sweepSegment (one line).
+template <typename T, int AXIS, int STRIDE, int LSTRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, int SLOPE,
+          int UNR, int LANES, class Emit>
+__device__ __forceinline__ void sweepAny(const T* box, int base, const TileK<T>& K, Emit&& emit) {
+    if constexpr (!EXACT && !LIM && sizeof(T) == 4) {
+        using V = typename std::conditional<LANES == 2, float2, float>::type;
+        lanes::Eos const e{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin};
+        sweepLanes<V, AXIS, STRIDE, LSTRIDE, BOXN, L, PLM, SLOPE, UNR>(box, base, e, SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter,
+                                                                      K.zero[AXIS], emit);
+    } else {
+        static_assert(LANES == 1, "two-lane sweeps need the FP32 fast form without a flux limiter");
+        sweepSegment<T, AXIS, STRIDE, BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K, emit);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the stage kernel
 // ---------------------------------------------------------------------------
@@ -566,8 +682,22 @@ struct StageCfg {
 
 constexpr unsigned kSpinLimit = 1u << 22;
 
-template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM, int SLOPE, int UNR>
-__global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs a, int slopeLim, int fluxLim) {
+// Resident CTAs per SM that a configuration's shared memory allows (228 KB per
+// SM, 1 KB reserved per CTA) and its thread count allows (2048 per SM).  The
+// stage kernel declares it as its minimum, so the compiler may use every
+// register that occupancy leaves (65536 / (CTAs x threads)) instead of
+// spilling to reach an occupancy the shared memory rules out anyway.
+constexpr int residentCtas(int nt, size_t smem) {
+    int const bySmem = (int)((size_t)228 * 1024 / (smem + 1024));
+    int const byThreads = 2048 / nt;
+    int const o = bySmem < byThreads ? bySmem : byThreads;
+    return o > 32 ? 32 : (o < 1 ? 1 : o);
+}
+
+template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM, int SLOPE, int UNR,
+          int OCC, int LANES>
+__global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ StageArgs a, int slopeLim, int fluxLim) {
+    static_assert(LANES == 1 || (DIM >= 2 && TX % 2 == 0 && TY % 2 == 0), "two-lane sweeps pair rows and columns");
     using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
     using G = typename Cfg::G;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -617,51 +747,57 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
         int const nx = I.n[0], ny = I.n[1], nz = I.n[2];
 
         // ---- all axes but the last: flux differences into D ----------------
+        // (LANES = 2: each thread sweeps two neighbouring lines in lockstep)
         if constexpr (DIM >= 2) {
 #pragma unroll 1
             for (int axis = 0; axis < DIM - 1; ++axis) {
                 if (axis == 0) {
-                    constexpr int nlines = TY * (DIM > 2 ? TZ : 1);
+                    // lines along x, indexed by (cy, cz); lanes are neighbouring rows
+                    constexpr int nlines = TY / LANES * (DIM > 2 ? TZ : 1);
                     constexpr int nseg = TX / L;
                     T const ar = K.area[0];
                     bool const skip = K.skip[0];
                     for (int t = tid; t < nlines * nseg; t += NT) {
                         int const line = t % nlines, seg = t / nlines;
-                        int const cy = line % TY, cz = line / TY;
+                        int const cy = (line % (TY / LANES)) * LANES, cz = line / (TY / LANES);
                         int const cx0 = seg * L;
                         if (x0 + cx0 >= nx || y0 + cy >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + (DIM > 2 ? 2 : 0)) * G::BY + (cy + 2)) * G::BX + (cx0 + 2);
                         T* Dl = D + (cz * TY + cy) * G::DPX + cx0;
-                        sweepSegment<T, 0, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K,
+                        sweepAny<T, 0, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES>(box, base, K,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
-                                for (int f = 0; f < 5; ++f) {
-                                    T d = T(0);
-                                    if (!skip) d = T(0) - (T(FR[f]) * ar - T(FL[f]) * ar);
-                                    Dl[f * G::DN + k] = d;
-                                }
+                                for (int l = 0; l < LANES; ++l)
+#pragma unroll
+                                    for (int f = 0; f < 5; ++f) {
+                                        T d = T(0);
+                                        if (!skip) d = fluxDiff<T, EXACT>(T(0), T(laneOf(FL[f], l)), T(laneOf(FR[f], l)), ar);
+                                        Dl[f * G::DN + l * G::DPX + k] = d;
+                                    }
                             });
                     }
                 } else if constexpr (DIM == 3) {
-                    // axis 1 of a 3D tile
-                    constexpr int nlines = TX * TZ;
+                    // axis 1 of a 3D tile: lines along y, indexed by (cx, cz); lanes are neighbouring columns
+                    constexpr int nlines = TX / LANES * TZ;
                     constexpr int nseg = TY / L;
                     T const ar = K.area[1];
                     bool const skip = K.skip[1];
                     for (int t = tid; t < nlines * nseg; t += NT) {
-                        int const cx = t % TX, rest = t / TX;
+                        int const cx = (t % (TX / LANES)) * LANES, rest = t / (TX / LANES);
                         int const cz = rest % TZ, seg = rest / TZ;
                         int const cy0 = seg * L;
                         if (x0 + cx >= nx || y0 + cy0 >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + 2) * G::BY + (cy0 + 2)) * G::BX + (cx + 2);
                         T* Dl = D + (cz * TY + cy0) * G::DPX + cx;
-                        sweepSegment<T, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K,
+                        sweepAny<T, 1, G::BX, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES>(box, base, K,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
-                                for (int f = 0; f < 5; ++f) {
-                                    T& d = Dl[f * G::DN + k * G::DPX];
-                                    if (!skip) d = d - (T(FR[f]) * ar - T(FL[f]) * ar);
-                                }
+                                for (int l = 0; l < LANES; ++l)
+#pragma unroll
+                                    for (int f = 0; f < 5; ++f) {
+                                        T& d = Dl[f * G::DN + k * G::DPX + l];
+                                        if (!skip) d = fluxDiff<T, EXACT>(d, T(laneOf(FL[f], l)), T(laneOf(FR[f], l)), ar);
+                                    }
                             });
                     }
                 }
@@ -672,7 +808,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
         // ---- last axis: sweep into D, then finish each of the segment's cells
         constexpr int AX = DIM - 1;
         constexpr int TA = AX == 0 ? TX : (AX == 1 ? TY : TZ);
-        constexpr int nlines = (TX * TY * TZ) / TA / (DIM < 2 ? TY : 1) / (DIM < 3 ? TZ : 1);
+        constexpr int nlines = (TX * TY * TZ) / TA / (DIM < 2 ? TY : 1) / (DIM < 3 ? TZ : 1) / LANES;
         constexpr int nseg = TA / L;
         constexpr int STRIDE_AX = AX == 0 ? 1 : (AX == 1 ? G::BX : G::BX * G::BY);
         constexpr int DSTRIDE_AX = AX == 0 ? 1 : (AX == 1 ? G::DPX : G::DPX * TY);
@@ -686,78 +822,172 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ StageArgs 
         T dtmin = fast::M<T>::inf();
         bool bad = false;
 
+        // the cell at global (gx, gy, gz), box index bi, accumulator Dc:
+        // Runge-Kutta combination, constrainU, store, ghost copies, stored
+        // derivative, CFL dt
+        auto finishCell = [&](int gx, int gy, int gz, int bi, const T* Dc) {
+            long long const idx = padIndex<DIM>(I, gx, gy, gz);
+            T u[5], deriv[5];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                deriv[f] = Dc[f * G::DN];
+                u[f] = T(0);
+            }
+            // u = sum alpha_k u^(k) + sum (beta_k dt) L(u^(k)) + (beta_cur dt) deriv
+            // (loops unrolled to their bound so the coefficients stay in registers)
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (m >= st.n_alpha) break;
+                int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
+                if (b == inBuf) {
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) u[f] = u[f] + box[f * G::BOXN + bi] * K.calpha[m];
+                } else {
+                    const T* src = reinterpret_cast<const T*>(I.buf[b]);
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * K.calpha[m];
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (m >= st.n_beta) break;
+                const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
+#pragma unroll
+                for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * K.cbeta[m];
+            }
+            if (useCur) {
+#pragma unroll
+                for (int f = 0; f < 5; ++f) u[f] = u[f] + deriv[f] * cbcur;
+            }
+            constrainCell<T, EXACT>(u, K);
+#pragma unroll
+            for (int f = 0; f < 5; ++f) out[f * I.plane + idx] = u[f];
+            // after constrainU a non-finite momentum shows in ETotal
+            bad |= !fast::M<T>::finite_(u[0] + u[4]);
+            scatterGhosts<T, DIM>(I, out, gx, gy, gz, u);
+            if (dstore) {
+#pragma unroll
+                for (int f = 0; f < 5; ++f) dstore[f * I.plane + idx] = deriv[f];
+            }
+            if (st.last) dtmin = fast::tmin(dtmin, dtCell<T, EXACT, DIM>(u, K, I));
+        };
+
+        // the fast form's epilogue, written with the lane operations: V = float
+        // finishes the cell (gx, gy, gz); V = float2 finishes it and its +x
+        // neighbour with packed arithmetic and 8-byte loads and stores
+        auto finishFast = [&](auto vtag, int gx, int gy, int gz, int bi, const T* Dc) {
+            using V = decltype(vtag);
+            constexpr int NL = lanes::nlanes<V>();
+            long long const idx = padIndex<DIM>(I, gx, gy, gz);
+            auto ld = [&](const T* p) -> V {
+                if constexpr (NL == 1) return *p;
+                else return *reinterpret_cast<const float2*>(p);
+            };
+            auto st_ = [&](T* p, V v) {
+                if constexpr (NL == 1) *p = v;
+                else *reinterpret_cast<float2*>(p) = v;
+            };
+            lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin};
+            V u[5], deriv[5];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                if constexpr (NL == 1) deriv[f] = Dc[f * G::DN];
+                else deriv[f] = make_float2(Dc[f * G::DN], Dc[f * G::DN + 1]);
+                u[f] = lanes::splat<V>(0.f);
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (m >= st.n_alpha) break;
+                int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
+                V const c = lanes::splat<V>(K.calpha[m]);
+                if (b == inBuf) {
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) u[f] = lanes::fma(ld(box + f * G::BOXN + bi), c, u[f]);
+                } else {
+                    const T* src = reinterpret_cast<const T*>(I.buf[b]);
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) u[f] = lanes::fma(ld(src + f * I.plane + idx), c, u[f]);
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (m >= st.n_beta) break;
+                const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
+                V const c = lanes::splat<V>(K.cbeta[m]);
+#pragma unroll
+                for (int f = 0; f < 5; ++f) u[f] = lanes::fma(ld(src + f * I.plane + idx), c, u[f]);
+            }
+            if (useCur) {
+                V const c = lanes::splat<V>(cbcur);
+#pragma unroll
+                for (int f = 0; f < 5; ++f) u[f] = lanes::fma(deriv[f], c, u[f]);
+            }
+            lanes::constrain<V>(u, le, K.invg1);
+#pragma unroll
+            for (int f = 0; f < 5; ++f) st_(out + f * I.plane + idx, u[f]);
+            if (dstore) {
+#pragma unroll
+                for (int f = 0; f < 5; ++f) st_(dstore + f * I.plane + idx, deriv[f]);
+            }
+            V dtv;
+            if (st.last) dtv = lanes::dtCell<V, DIM>(u, le, K.gdx);
+#pragma unroll
+            for (int l = 0; l < NL; ++l) {
+                T uu[5];
+#pragma unroll
+                for (int f = 0; f < 5; ++f) uu[f] = lanes::lane(u[f], l);
+                // after constrainU a non-finite momentum shows in ETotal
+                bad |= !fast::M<T>::finite_(uu[0] + uu[4]);
+                scatterGhosts<T, DIM>(I, out, gx + l, gy, gz, uu);
+                if (st.last) dtmin = fast::tmin(dtmin, lanes::lane(dtv, l));
+            }
+        };
+
         for (int t = tid; t < nlines * nseg; t += NT) {
             int cx, cy, cz, seg;
             if (DIM == 1) { cx = 0; cy = 0; cz = 0; seg = t; }
-            else if (DIM == 2) { cx = t % TX; seg = t / TX; cy = 0; cz = 0; }
-            else { cx = t % TX; cy = (t / TX) % TY; seg = t / (TX * TY); cz = 0; }
+            else if (DIM == 2) { cx = (t % (TX / LANES)) * LANES; seg = t / (TX / LANES); cy = 0; cz = 0; }
+            else { cx = (t % (TX / LANES)) * LANES; cy = (t / (TX / LANES)) % TY; seg = t / (TX / LANES * TY); cz = 0; }
             int c0[3] = {cx, cy, cz};
             c0[AX] = seg * L;
             int const gx0 = x0 + c0[0], gy0 = y0 + c0[1], gz0 = z0 + c0[2];
             if (gx0 >= nx || gy0 >= ny || gz0 >= nz) continue;
             int const base = ((c0[2] + (DIM > 2 ? 2 : 0)) * G::BY + (c0[1] + (DIM > 1 ? 2 : 0))) * G::BX + (c0[0] + 2);
             T* Dl = D + (c0[2] * TY + c0[1]) * G::DPX + c0[0];
-            sweepSegment<T, AX, STRIDE_AX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K,
+            sweepAny<T, AX, STRIDE_AX, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES>(box, base, K,
                 [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
-                    for (int f = 0; f < 5; ++f) {
-                        T& d = Dl[f * G::DN + k * DSTRIDE_AX];
-                        T dv = DIM > 1 ? d : T(0);
-                        if (!skipF) dv = dv - (T(FR[f]) * arF - T(FL[f]) * arF);
-                        d = dv;
-                    }
+                    for (int l = 0; l < LANES; ++l)
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) {
+                            T& d = Dl[f * G::DN + k * DSTRIDE_AX + l];
+                            T dv = DIM > 1 ? d : T(0);
+                            if (!skipF) dv = fluxDiff<T, EXACT>(dv, T(laneOf(FL[f], l)), T(laneOf(FR[f], l)), arF);
+                            d = dv;
+                        }
                 });
-            // the cells of this segment: Runge-Kutta combination, constrainU,
-            // store, ghost copies, stored derivative, CFL dt
             int const gA0 = AX == 0 ? gx0 : (AX == 1 ? gy0 : gz0);
             int const nA = AX == 0 ? nx : (AX == 1 ? ny : nz);
             int const kmax = nA - gA0 < L ? nA - gA0 : L;
+            if constexpr (EXACT) {
 #pragma unroll 1
-            for (int k = 0; k < kmax; ++k) {
-                int g[3] = {gx0, gy0, gz0};
-                g[AX] += k;
-                long long const idx = padIndex<DIM>(I, g[0], g[1], g[2]);
-                T u[5], deriv[5];
-#pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    deriv[f] = Dl[f * G::DN + k * DSTRIDE_AX];
-                    u[f] = T(0);
+                for (int k = 0; k < kmax; ++k) {
+                    int g[3] = {gx0, gy0, gz0};
+                    g[AX] += k;
+                    finishCell(g[0], g[1], g[2], base + k * STRIDE_AX, Dl + k * DSTRIDE_AX);
                 }
-                // u = sum alpha_k u^(k) + sum (beta_k dt) L(u^(k)) + (beta_cur dt) deriv
-                for (int m = 0; m < st.n_alpha; ++m) {
-                    int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
-                    if (b == inBuf) {
-#pragma unroll
-                        for (int f = 0; f < 5; ++f) u[f] = u[f] + box[f * G::BOXN + base + k * STRIDE_AX] * K.calpha[m];
-                    } else {
-                        const T* src = reinterpret_cast<const T*>(I.buf[b]);
-#pragma unroll
-                        for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * K.calpha[m];
-                    }
+            } else {
+                // LANES = 2: the line pair, unless the second line lies beyond the grid
+                bool const pair = LANES == 2 && gx0 + 1 < nx;
+#pragma unroll 1
+                for (int k = 0; k < kmax; ++k) {
+                    int g[3] = {gx0, gy0, gz0};
+                    g[AX] += k;
+                    if (LANES == 2 && pair) finishFast(float2{}, g[0], g[1], g[2], base + k * STRIDE_AX, Dl + k * DSTRIDE_AX);
+                    else finishFast(T{}, g[0], g[1], g[2], base + k * STRIDE_AX, Dl + k * DSTRIDE_AX);
                 }
-                for (int m = 0; m < st.n_beta; ++m) {
-                    const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
-#pragma unroll
-                    for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * K.cbeta[m];
-                }
-                if (useCur) {
-#pragma unroll
-                    for (int f = 0; f < 5; ++f) u[f] = u[f] + deriv[f] * cbcur;
-                }
-                constrainCell<T, EXACT>(u, K);
-#pragma unroll
-                for (int f = 0; f < 5; ++f) out[f * I.plane + idx] = u[f];
-                // after constrainU a non-finite momentum shows in ETotal
-                bad |= !fast::M<T>::finite_(u[0] + u[4]);
-                scatterGhosts<T, DIM>(I, out, g[0], g[1], g[2], u);
-                if (dstore) {
-#pragma unroll
-                    for (int f = 0; f < 5; ++f) dstore[f * I.plane + idx] = deriv[f];
-                }
-                if (st.last) dtmin = fast::tmin(dtmin, dtCell<T, EXACT, DIM>(u, K, I));
             }
         }
-
         // one FP64 atomicMin per warp for the next step's CFL dt
         if (st.last) {
 #pragma unroll
@@ -906,6 +1136,8 @@ struct StageLauncher {
     int slope;       // slope limiter compiled in, or -1 (any, dispatched at run time)
     int variant;     // tile-shape candidate index
     int tx, ty, tz, nthreads;
+    int seg, unroll, min_ctas;   // segment length, sliding-window unroll (0: full), CTAs per SM compiled for
+    int lanes;                   // lines per thread (2: packed FP32 pairs)
     size_t smem;
     void (*launch)(const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s);
     int (*occupancy)();   // CTAs per SM (sets the smem attribute first); <= 0 on error

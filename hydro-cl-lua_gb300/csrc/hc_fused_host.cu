@@ -11,10 +11,12 @@
 // buffer is reallocated or the set of dimensions changes).
 #include "hc_internal.h"
 #include "hc_fused.cuh"
+#include "hc_pool.h"
 
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -182,6 +184,7 @@ struct FusedSet {
     bool graph_valid = false;
     int graph_dims_mask = 0;
     std::string tune_log;          // per-variant timings of the last autotune
+    DevicePool pool;               // instance state buffers
 };
 
 static const StageLauncher* find_launcher(const FusedScheme& sch, int dim, int variant) {
@@ -278,7 +281,7 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
 void fused_destroy(FusedSet* f) {
     if (!f) return;
     if (f->stream) cudaStreamSynchronize(f->stream);
-    for (Slot& s : f->slots) if (s.mem) cudaFree(s.mem);
+    f->pool.release_all();
     cudaFree(f->d_inst);
     cudaFree(f->d_ctl);
     cudaFree(f->d_tmaps);
@@ -406,6 +409,34 @@ int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int res
     return HC_OK;
 }
 
+int fused_init_state(FusedSet* f, int slot, const hc_init& ic) {
+    Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    HC_CHECK(init_validate(ic, S.d));
+    const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
+    HC_CHECK(ensure_staging(f, layout_bytes(S.cells, HC_LAYOUT_AOS6_F64)));
+    HC_CHECK(init_fill(ic, S.d, static_cast<double*>(f->staging), f->stream));
+    // from here on exactly the path of a host upload (fused_set_state with reset)
+    int const b = state_buf(f, slot);
+    fz::k_restart<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
+    A->xfer(f->d_inst, slot, b, f->staging, HC_LAYOUT_AOS6_F64, 0, f->stream);
+    A->constrain(f->d_inst, slot, b, f->stream);
+    A->fill_ghosts(f->d_inst, slot, b, f->stream);
+    fz::k_reset_dtmin<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
+    A->calc_dt(f->d_inst, f->d_ctl, slot, b, f->stream);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int fused_get_state_dev(FusedSet* f, int slot, void* dev, int layout) {
+    Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    find_aux(f->sch.precision, S.dim)->xfer(f->d_inst, slot, state_buf(f, slot), dev, layout, 1, f->stream);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
 int fused_get_state(FusedSet* f, int slot, void* host, int layout) {
     Slot& S = f->slots[slot];
     if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
@@ -421,7 +452,7 @@ int fused_get_state(FusedSet* f, int slot, void* host, int layout) {
 }
 
 int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout, double t_end, long long max_steps,
-              int stop_on_error) {
+              int stop_on_error, const hc_init* init) {
     if (slot < 0 || slot >= f->max_slots || f->slots[slot].used) return fail(HC_ERR_STATE, "slot unavailable");
     HC_CHECK(validate(f, d));
     Slot& S = f->slots[slot];
@@ -433,7 +464,7 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     size_t const planeBytes = round_up(plane * f->esize, 256);
     int const nb = f->plan[0].n_state_bufs, nd = f->plan[0].n_deriv_bufs;
     S.bytes = planeBytes * 5 * (nb + nd);
-    cudaError_t e = cudaMalloc(&S.mem, S.bytes);
+    cudaError_t e = f->pool.alloc(S.bytes, &S.mem);
     if (e != cudaSuccess) { S.mem = nullptr; return cuda_fail(e, "cudaMalloc (instance state)"); }
     HC_CUDA(cudaMemsetAsync(S.mem, 0, S.bytes, f->stream));
     DevInst& I = S.inst;
@@ -494,6 +525,7 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     HC_CUDA(cudaMemcpyAsync(f->d_ctl + slot, &c, sizeof(DevCtl), cudaMemcpyHostToDevice, f->stream));
     int r = encode_maps(f, slot);
     if (r == HC_OK && host) r = fused_set_state(f, slot, host, layout, 1);
+    if (r == HC_OK && !host && init) r = fused_init_state(f, slot, *init);
     if (r != HC_OK) {
         fused_remove(f, slot);
         return r;
@@ -507,8 +539,9 @@ int fused_remove(FusedSet* f, int slot) {
     if (slot < 0 || slot >= f->max_slots) return fail(HC_ERR_INVALID, "slot");
     Slot& S = f->slots[slot];
     if (!S.used) return HC_OK;
-    HC_CUDA(cudaStreamSynchronize(f->stream));
-    cudaFree(S.mem);
+    // no synchronisation: later users of the range are ordered behind the
+    // work already on the stream
+    f->pool.release(S.mem, S.bytes);
     S.mem = nullptr;
     S.used = false;
     DevCtl c;
@@ -719,8 +752,15 @@ int fused_constrain_u(FusedSet* f, int slot) {
     return HC_OK;
 }
 
+// The per-slot status fields sit at the head of DevCtl; a status read copies
+// only those bytes of each slot (one strided copy).
+constexpr size_t kStatusBytes = 64;
+static_assert(offsetof(DevCtl, rot) + sizeof(int) <= kStatusBytes, "status fields beyond the copied head");
+static_assert(offsetof(DevCtl, dtmin) + 2 * sizeof(unsigned long long) <= kStatusBytes, "dtmin beyond the copied head");
+
 int fused_slot_info(FusedSet* f, std::vector<SlotInfo>& out) {
-    HC_CUDA(cudaMemcpyAsync(f->h_ctl, f->d_ctl, sizeof(DevCtl) * f->max_slots, cudaMemcpyDeviceToHost, f->stream));
+    HC_CUDA(cudaMemcpy2DAsync(f->h_ctl, sizeof(DevCtl), f->d_ctl, sizeof(DevCtl), kStatusBytes, f->max_slots,
+                              cudaMemcpyDeviceToHost, f->stream));
     HC_CUDA(cudaStreamSynchronize(f->stream));
     out.resize(f->max_slots);
     for (int s = 0; s < f->max_slots; ++s) {
@@ -885,8 +925,10 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
             cudaEventDestroy(e1);
             fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->betas);
             HC_CUDA(cudaStreamSynchronize(f->stream));
-            log << "# " << key << " variant " << v << " tile " << f->launcher[dim - 1]->tx << "x" << f->launcher[dim - 1]->ty
-                << "x" << f->launcher[dim - 1]->tz << " threads " << f->launcher[dim - 1]->nthreads << " ms/stage " << ms / reps << "\n";
+            const StageLauncher* Lc = f->launcher[dim - 1];
+            log << "# " << key << " variant " << v << " tile " << Lc->tx << "x" << Lc->ty << "x" << Lc->tz << " threads "
+                << Lc->nthreads << " seg " << Lc->seg << " unroll " << Lc->unroll << " ctas/SM " << Lc->min_ctas
+                << " lanes " << Lc->lanes << " slope " << Lc->slope << " ms/stage " << ms / reps << "\n";
             if (ms < bestMs) { bestMs = ms; best = v; }
         }
         f->tune_log += log.str();
@@ -915,6 +957,7 @@ void register_f32_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2a(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2c(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_d2d(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -925,6 +968,7 @@ void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>
     register_f32_d2a(st, aux);
     register_f32_d2b(st, aux);
     register_f32_d2c(st, aux);
+    register_f32_d2d(st, aux);
     register_f32_d3(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);

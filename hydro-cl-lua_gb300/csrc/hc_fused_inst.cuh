@@ -8,10 +8,14 @@
 namespace hc {
 namespace fz {
 
+// OCC: minimum resident CTAs per SM the kernel is compiled for (0: as many as
+// its shared memory and thread count allow).  LANES: lines each thread sweeps
+// at once (2: packed FP32 pairs).
 template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM,
-          int SLOPE = -1, int UNR = 0>
+          int SLOPE = -1, int UNR = 0, int OCC = 0, int LANES = 1>
 void add_stage(std::vector<StageLauncher>& v) {
     using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
+    constexpr int K = OCC > 0 ? OCC : residentCtas(NT, Cfg::SMEM);
     StageLauncher sl;
     sl.precision = PREC;
     sl.dim = DIM;
@@ -23,12 +27,16 @@ void add_stage(std::vector<StageLauncher>& v) {
     sl.ty = TY;
     sl.tz = TZ;
     sl.nthreads = NT;
+    sl.seg = L;
+    sl.unroll = UNR;
+    sl.min_ctas = K;
+    sl.lanes = LANES;
     sl.smem = Cfg::SMEM;
     sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
-        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR, K, LANES><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
     };
     sl.occupancy = []() -> int {
-        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR>;
+        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR, K, LANES>;
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NT, Cfg::SMEM) != cudaSuccess) return -1;
@@ -44,21 +52,22 @@ inline unsigned aux_blocks(long long n) {
 
 // The FP32 PLM kernels for the slope limiters the configurations use, plus the
 // generic one: minmod, van Leer (comment form), monotized central, superbee.
-template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, int UNR = 0>
+template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, int UNR = 0, int OCC = 0,
+          int LANES = 1>
 void add_plm_set(std::vector<StageLauncher>& v) {
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1, UNR>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MINMOD, UNR>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MONOTIZED_CENTRAL, UNR>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS, UNR>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_SUPERBEE, UNR>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MINMOD, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MONOTIZED_CENTRAL, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_SUPERBEE, UNR, OCC, LANES>(v);
 }
 
 // Extra schedules for one compiled-in limiter (the batched configuration's)
 // and the generic kernel.
-template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, int UNR>
+template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, int UNR, int OCC = 0, int LANES = 1>
 void add_plm_pair(std::vector<StageLauncher>& v) {
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1, UNR>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS, UNR>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS, UNR, OCC, LANES>(v);
 }
 
 template <typename T, int PREC, int DIM, bool EXACT>

@@ -119,10 +119,21 @@ void fused_destroy(FusedSet* f);
 size_t fused_instance_bytes(const FusedSet* f, const hc_solver_desc& d);
 // stop_on_error: a non-finite state or dt ends the instance (batches); the
 // single-solver form steps on like the reference and only records the status.
+// The initial state comes from `host` (in `layout`), else from `init` (built
+// on the device), else it stays zero until a set_state.
 int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout,
-              double t_end, long long max_steps, int stop_on_error);
+              double t_end, long long max_steps, int stop_on_error, const hc_init* init = nullptr);
 int fused_remove(FusedSet* f, int slot);
 int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int reset);
+// resetState from a device-built initial condition
+int fused_init_state(FusedSet* f, int slot, const hc_init& ic);
+int plain_init_state(PlainSolver* p, const hc_init& ic, const hc_solver_desc& d);
+int plain_expand_full(const hc_solver_desc& d, const void* interior_dev, int layout, double* full_dev, cudaStream_t s);
+// the slot's interior state into device memory (layout as for host I/O)
+int fused_get_state_dev(FusedSet* f, int slot, void* dev, int layout);
+// initial conditions (hc_init.cu): the interior in AoS-6 FP64, x fastest, into device memory
+int init_validate(const hc_init& ic, const hc_solver_desc& d);
+int init_fill(const hc_init& ic, const hc_solver_desc& d, double* dst, cudaStream_t s);
 int fused_get_state(FusedSet* f, int slot, void* host, int layout);
 // Runs `steps` updates of every live instance (device-side completion tests).
 int fused_steps(FusedSet* f, int steps);

@@ -449,6 +449,50 @@ int plain_set_interior(PlainSolver* s, const void* host, int layout) {
     return HC_OK;
 }
 
+// The reference's UBuf (AoS-6, ghosts included) of a solver described by d,
+// from its interior cells in device memory: the interior is placed and the
+// ghosts filled by the plain form's boundary kernels (gridsolver.lua:638-780,
+// x then y then z, corners included).  Used to export the state of the fused
+// forms, which keep no corner ghosts, in the reference's layout.
+int plain_expand_full(const hc_solver_desc& d, const void* interior_dev, int layout, double* full_dev, cudaStream_t stream) {
+    PlainParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.dim = d.dim;
+    for (int k = 0; k < 3; ++k) {
+        int const n = k < d.dim ? d.n[k] : 1;
+        p.gs[k] = k < d.dim ? n + 2 * kGhost : 1;
+        p.grid_dx[k] = (d.maxs[k] - d.mins[k]) / (double)n;
+    }
+    p.stepsize[0] = 1;
+    p.stepsize[1] = p.gs[0];
+    p.stepsize[2] = p.gs[0] * p.gs[1];
+    p.numCells = (long long)p.gs[0] * p.gs[1] * p.gs[2];
+    for (int k = 0; k < 6; ++k) p.bc[k] = d.boundary[k];
+    p.gamma = d.gamma;
+    p.rhoMin = d.rho_min;
+    p.PMin = d.p_min;
+    long long const n = interior_count(p);
+    HC_CUDA(cudaMemsetAsync(full_dev, 0, (size_t)p.numCells * sizeof(Cons), stream));
+    k_interior_xfer<<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256, 0, stream>>>(
+        p, reinterpret_cast<Cons*>(full_dev), const_cast<void*>(interior_dev), layout, 0);
+    for (int side = 0; side < p.dim; ++side) {
+        int const o1 = (side + 1) % 3, o2 = (side + 2) % 3;
+        long long const lines = (long long)p.gs[o1] * p.gs[o2];
+        k_boundary<<<(unsigned)((lines + 127) / 128), 128, 0, stream>>>(p, reinterpret_cast<Cons*>(full_dev), side);
+    }
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int plain_init_state(PlainSolver* s, const hc_init& ic, const hc_solver_desc& d) {
+    long long const n = interior_count(s->p);
+    HC_CHECK(init_fill(ic, d, static_cast<double*>(s->staging), s->stream));
+    k_interior_xfer<<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256, 0, s->stream>>>(
+        s->p, s->U, s->staging, HC_LAYOUT_AOS6_F64, 0);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
 int plain_get_interior(PlainSolver* s, void* host, int layout) {
     long long const n = interior_count(s->p);
     k_interior_xfer<<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256, 0, s->stream>>>(s->p, s->U, s->staging, layout, 1);

@@ -89,6 +89,14 @@ class BatchStats(ctypes.Structure):
                 ("tile", (ctypes.c_int * 3) * 3)]
 
 
+class Init(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("reserved", ctypes.c_int), ("seed", ctypes.c_ulonglong),
+                ("p", ctypes.c_double * 16)]
+
+
+INIT_KINDS = {"sod": 0, "blast": 1, "quadrant": 2, "kelvin-helmholtz": 3}
+
+
 # every entry point of include/hydrocuda.h with its argument types
 _vp, _dp, _ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
 PROTOTYPES = {
@@ -99,9 +107,11 @@ PROTOTYPES = {
     "hc_context_destroy": (_ip, [_vp]),
     "hc_host_alloc": (_ip, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
     "hc_host_free": (_ip, [_vp]),
+    "hc_init_defaults": (_ip, [_ip, ctypes.POINTER(Init)]),
     "hc_solver_create": (_ip, [_vp, ctypes.POINTER(SolverDesc), ctypes.POINTER(_vp)]),
     "hc_solver_destroy": (_ip, [_vp]),
     "hc_solver_reset_state": (_ip, [_vp, _vp, _ip]),
+    "hc_solver_init_state": (_ip, [_vp, ctypes.POINTER(Init)]),
     "hc_solver_set_state": (_ip, [_vp, _vp, _ip, _ip]),
     "hc_solver_get_state": (_ip, [_vp, _vp, _ip, _ip]),
     "hc_solver_boundary": (_ip, [_vp]),
@@ -118,6 +128,8 @@ PROTOTYPES = {
     "hc_batch_destroy": (_ip, [_vp]),
     "hc_batch_admit": (_ip, [_vp, ctypes.POINTER(SolverDesc), _vp, _ip, ctypes.c_double, ctypes.c_longlong,
                              ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_int)]),
+    "hc_batch_admit_init": (_ip, [_vp, ctypes.POINTER(SolverDesc), ctypes.POINTER(Init), ctypes.c_double,
+                                  ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_int)]),
     "hc_batch_step": (_ip, [_vp, _ip, ctypes.POINTER(ctypes.c_int)]),
     "hc_batch_step_timed": (_ip, [_vp, _ip, _dp, _ip, _dp]),
     "hc_batch_poll": (_ip, [_vp, ctypes.POINTER(Done), _ip, ctypes.POINTER(ctypes.c_int)]),
@@ -203,6 +215,33 @@ def _index(table, name, what):
         return table.index(name)
     except ValueError:
         raise ValueError("unknown %s %r" % (what, name))
+
+
+def make_init(kind, **params):
+    """An initial condition for the device (hc_init).  kind: "sod" (rhoL, PL, rhoR,
+    PR), "blast" (radius, Pin, Pout, rho), "quadrant" (q: 4 x (rho, vx, vy, P), as
+    random_quadrants returns), "kelvin-helmholtz" (seed, noise); parameters not
+    given keep the library's defaults.  The states equal those of sod_state,
+    blast_state, quadrant_state and kelvin_helmholtz_state bit for bit."""
+    L = load_library()
+    ic = Init()
+    _check(L.hc_init_defaults(INIT_KINDS[kind], ctypes.byref(ic)))
+    names = {"sod": ("rhoL", "PL", "rhoR", "PR"), "blast": ("radius", "Pin", "Pout", "rho"),
+             "kelvin-helmholtz": ("noise",), "quadrant": ()}[kind]
+    for k, v in params.items():
+        if k == "seed" and kind == "kelvin-helmholtz":
+            ic.seed = int(v)
+        elif k == "q" and kind == "quadrant":
+            flat = [float(x) for quad in v for x in quad]
+            if len(flat) != 16:
+                raise ValueError("quadrant: q must hold 4 x (rho, vx, vy, P)")
+            for i, x in enumerate(flat):
+                ic.p[i] = x
+        elif k in names:
+            ic.p[names.index(k)] = float(v)
+        else:
+            raise ValueError("unknown parameter %r for %s" % (k, kind))
+    return ic
 
 
 def make_desc(args):
@@ -305,6 +344,11 @@ class Solver:
         """resetState with the given interior conserved state (applyInitCond's output)."""
         a = _as_layout(cons, layout, self.num_interior)
         _check(self.L.hc_solver_reset_state(self.h, a.ctypes.data, LAYOUTS[layout]))
+
+    def initState(self, kind, **params):
+        """resetState with the initial condition built on the device (see make_init)."""
+        ic = make_init(kind, **params)
+        _check(self.L.hc_solver_init_state(self.h, ctypes.byref(ic)))
 
     def setState(self, cons, layout="aos6", withGhosts=False):
         if withGhosts:
@@ -418,6 +462,27 @@ class Batch:
         self.slot_desc[slot.value] = desc
         return slot.value
 
+    def admit_init(self, args, kind, t_end, max_steps=0, tag=0, **params):
+        """admit with the initial condition built on the device (see make_init)."""
+        a = dict(self.scheme)
+        a.update(args)
+        desc = make_desc(a)
+        ic = make_init(kind, **params)
+        slot = ctypes.c_int(-1)
+        _check(self.L.hc_batch_admit_init(self.h, ctypes.byref(desc), ctypes.byref(ic), float(t_end), int(max_steps),
+                                          int(tag), ctypes.byref(slot)))
+        self.slot_desc[slot.value] = desc
+        return slot.value
+
+    def try_admit_init(self, args, kind, t_end, max_steps=0, tag=0, **params):
+        """Like admit_init, but returns None when the budget or the slot table refuses."""
+        try:
+            return self.admit_init(args, kind, t_end, max_steps, tag, **params)
+        except HydroCudaError as e:
+            if e.code in (-4, -5):
+                return None
+            raise
+
     def try_admit(self, args, cons, t_end, max_steps=0, tag=0, layout="aos6"):
         """Like admit, but returns None when the budget or the slot table refuses."""
         try:
@@ -447,15 +512,20 @@ class Batch:
         return [dict(slot=arr[i].slot, status=arr[i].status, tag=arr[i].tag, steps=arr[i].steps, t=arr[i].t)
                 for i in range(n.value)]
 
-    def fetch(self, slot, layout="aos6"):
+    def fetch(self, slot, layout="aos6", out=None):
+        """The slot's interior state in `layout`; written into `out` when given
+        (a C-contiguous array of the layout's dtype and size, e.g. a view of
+        pinned host memory), else into a new array."""
         desc = self.slot_desc[slot]
         n = interior_count(desc)
-        if layout == "aos6":
-            out = np.empty((n, 6), dtype=np.float64)
-        elif layout == "soa5":
-            out = np.empty((5, n), dtype=np.float64)
-        else:
-            out = np.empty((5, n), dtype=np.float32)
+        shape, dtype = {"aos6": ((n, 6), np.float64), "soa5": ((5, n), np.float64),
+                        "soa5_f32": ((5, n), np.float32)}[layout]
+        if out is None:
+            out = np.empty(shape, dtype=dtype)
+        elif out.dtype != dtype or out.size != shape[0] * shape[1] or not out.flags["C_CONTIGUOUS"] \
+                or not out.flags["WRITEABLE"]:
+            raise ValueError("fetch: out must be a writeable C-contiguous %s array of %d values" % (
+                np.dtype(dtype).name, shape[0] * shape[1]))
         _check(self.L.hc_batch_fetch(self.h, int(slot), out.ctypes.data, LAYOUTS[layout]))
         return out
 

@@ -22,14 +22,22 @@ import hydrocuda
 
 
 class Request:
-    __slots__ = ("arrival", "args", "cons", "t_end", "tag", "admitted", "finished", "steps", "t", "status", "result")
+    """One solve: `cons` is the initial interior state in `layout`, or a
+    callable returning it (called once, when the request is first offered for
+    admission, so a long stream need not hold every state in host memory), or
+    None with `init` = (kind, params) naming an initial condition the library
+    builds on the device (hydrocuda.make_init)."""
+    __slots__ = ("arrival", "args", "cons", "t_end", "tag", "layout", "init", "admitted", "finished", "steps", "t",
+                 "status", "result")
 
-    def __init__(self, arrival, args, cons, t_end, tag):
+    def __init__(self, arrival, args, cons, t_end, tag, layout="aos6", init=None):
         self.arrival = float(arrival)
         self.args = args
         self.cons = cons
         self.t_end = float(t_end)
         self.tag = int(tag)
+        self.layout = layout
+        self.init = init
         self.admitted = None
         self.finished = None
         self.steps = 0
@@ -43,7 +51,8 @@ class Server:
 
     steps_per_tick: updates per hc_batch_step call between admission / poll
     passes (larger values amortise host round trips, smaller ones admit and
-    retire sooner).  keep_results: fetch the final state of every solve.
+    retire sooner).  keep_results: fetch the final state of every solve (True),
+    of none (False), or of the requests whose tags are in the given set.
     """
 
     def __init__(self, batch, steps_per_tick=8, keep_results=True, result_layout="aos6"):
@@ -76,7 +85,12 @@ class Server:
             # admit every arrived request that fits
             while pending and pending[0].arrival <= now:
                 r = pending[0]
-                slot = self.batch.try_admit(r.args, r.cons, r.t_end, tag=r.tag)
+                if r.init is not None:
+                    slot = self.batch.try_admit_init(r.args, r.init[0], r.t_end, tag=r.tag, **r.init[1])
+                else:
+                    if callable(r.cons):
+                        r.cons = r.cons()
+                    slot = self.batch.try_admit(r.args, r.cons, r.t_end, tag=r.tag, layout=r.layout)
                 if slot is None:
                     if live == 0:
                         raise RuntimeError("request %d does not fit an empty batch" % r.tag)
@@ -98,7 +112,8 @@ class Server:
                     r.steps = ev["steps"]
                     r.t = ev["t"]
                     r.status = ev["status"]
-                    if self.keep_results:
+                    keep = self.keep_results
+                    if keep is True or (keep and not isinstance(keep, bool) and r.tag in keep):
                         r.result = self.batch.fetch(slot, self.result_layout)
                     self.batch.retire(slot)
                     r.finished = clock()
@@ -120,13 +135,25 @@ def latency_summary(done):
     }
 
 
-def synthetic_stream(count, rate_hz, seed=5, scale=1.0, gamma=1.4):
+def _in_layout(cons, layout):
+    if layout == "aos6":
+        return cons
+    a = np.ascontiguousarray(cons[:, :5].T)
+    return a.astype(np.float32) if layout == "soa5_f32" else a
+
+
+def synthetic_stream(count, rate_hz, seed=5, scale=1.0, gamma=1.4, lazy=False, layout="aos6", device_init=False):
     """Poisson arrivals (mean rate_hz) of 1D / 2D / 3D Euler solves.
 
     40 % 1D with N ~ logU[512, 65536], 45 % 2D with N ~ logU[128, 1024],
     15 % 3D with N ~ logU[64, 192] (N scaled by `scale` for reduced runs);
     the initial state is uniformly one of Sod (along x), blast, quadrant;
     t_end ~ U(0.05, 0.2).  Scheme: plm cons + minmod, Runge-Kutta 2, CFL 0.3.
+    lazy: each request carries a callable that builds its state on demand
+    (every random draw is still made here, in stream order).  layout: the
+    state layout handed to admission ("aos6", "soa5", "soa5_f32").
+    device_init: each request names its initial condition instead, and the
+    library builds the (identical) state on the device at admission.
     """
     rng = hydrocuda.SplitMix64(seed)
     t = 0.0
@@ -148,10 +175,18 @@ def synthetic_stream(count, rate_hz, seed=5, scale=1.0, gamma=1.4):
                     usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2", cfl=.3,
                     eqnArgs={"heatCapacityRatio": gamma})
         if kind == 0 or dim == 1 and kind == 2:
-            cons = hydrocuda.sod_state(args)
-        elif kind == 1:
-            cons = hydrocuda.blast_state(args)
+            make = (lambda a: lambda: hydrocuda.sod_state(a))(args)
+            init = ("sod", {})
+        elif kind == 1 or dim != 2:
+            make = (lambda a: lambda: hydrocuda.blast_state(a))(args)
+            init = ("blast", {})
         else:
-            cons = hydrocuda.quadrant_state(args, hydrocuda.random_quadrants(rng)) if dim == 2 else hydrocuda.blast_state(args)
-        out.append(Request(t, args, cons, t_end, tag))
+            q = hydrocuda.random_quadrants(rng)
+            make = (lambda a, q: lambda: hydrocuda.quadrant_state(a, q))(args, q)
+            init = ("quadrant", {"q": q})
+        if device_init:
+            out.append(Request(t, args, None, t_end, tag, init=init))
+            continue
+        build = (lambda m: lambda: _in_layout(m(), layout))(make)
+        out.append(Request(t, args, build if lazy else build(), t_end, tag, layout))
     return out

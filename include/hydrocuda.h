@@ -137,6 +137,30 @@ typedef struct hc_solver_desc {
     double fixed_dt;         /* > 0: useFixedDT with this dt; <= 0: CFL dt */
 } hc_solver_desc;
 
+/* Initial conditions generated on the device (the reference builds every
+ * initial state with its initCond kernel, solverbase.lua:2094-2136).  p[] by
+ * kind (hc_init_defaults fills the defaults):
+ *   SOD               rhoL, PL, rhoR, PR; left where x < mid on every active axis
+ *                     (hydro/init/euler.lua:742-752)
+ *   BLAST             radius, Pin, Pout, rho; P = Pin where |x| < radius
+ *   QUADRANT          4 x (rho, vx, vy, P) in the reference's quadrant order
+ *                     (+x+y, -x+y, -x-y, +x-y) (hydro/init/euler.lua:249-283); 2D
+ *   KELVIN_HELMHOLTZ  noise; |y| < .25: rho 2, vx .5, else rho 1, vx -.5; P 2.5;
+ *                     vy = noise * U(-1, 1) from SplitMix64(seed), one draw per
+ *                     cell in x-fastest order; 2D
+ * The states equal, bit for bit, the host generators of the Python binding. */
+#define HC_INIT_SOD               0
+#define HC_INIT_BLAST             1
+#define HC_INIT_QUADRANT          2
+#define HC_INIT_KELVIN_HELMHOLTZ  3
+
+typedef struct hc_init {
+    int                kind;     /* HC_INIT_* */
+    int                reserved;
+    unsigned long long seed;     /* KELVIN_HELMHOLTZ */
+    double             p[16];
+} hc_init;
+
 typedef struct hc_context hc_context;
 typedef struct hc_solver  hc_solver;
 typedef struct hc_batch   hc_batch;
@@ -149,12 +173,16 @@ const char* hc_version(void);
 const char* hc_last_error(void);
 /* Number of visible CUDA devices. */
 int hc_device_count(int* count);
-/* One context per device; owns the streams the handles below use. */
+/* One context per device; owns the streams the handles below use.
+   hc_context_destroy releases the caller's reference: the context itself
+   lives on until every solver and batch made on it is destroyed too. */
 int hc_context_create(int device, hc_context** out);
 int hc_context_destroy(hc_context* ctx);
 /* Pinned host memory for fast state transfers (optional). */
 int hc_host_alloc(size_t bytes, void** out);
 int hc_host_free(void* p);
+/* The default parameters of an initial condition. */
+int hc_init_defaults(int kind, hc_init* out);
 
 /* ---- single solver (FiniteVolumeSolver with flux='roe', eqn='euler') ---- */
 
@@ -165,8 +193,14 @@ int hc_solver_destroy(hc_solver* s);
 /* resetState after applyInitCond (solverbase.lua:2094-2114): writes the
  * interior conserved state, fills the ghosts, applies constrainU, sets t = 0. */
 int hc_solver_reset_state(hc_solver* s, const void* cons, int layout);
-/* Raw state I/O.  with_ghosts = 1 reads/writes the full grid including the
- * numGhost = 2 layers (AOS6_F64 only); 0 the interior only. */
+/* resetState with the initial condition built on the device (applyInitCond,
+ * solverbase.lua:2130-2136): no host array, no upload. */
+int hc_solver_init_state(hc_solver* s, const hc_init* init);
+/* Raw state I/O.  with_ghosts = 1 reads/writes the reference's whole UBuf,
+ * numGhost = 2 layers included (AOS6_F64 only); 0 the interior only.  The
+ * plain form holds the UBuf itself; the fused forms return their interior
+ * with the ghosts filled by the boundary rules (gridsolver.lua:638-780), and
+ * take the interior of a UBuf written to them. */
 int hc_solver_set_state(hc_solver* s, const void* cons, int layout, int with_ghosts);
 int hc_solver_get_state(hc_solver* s, void* cons, int layout, int with_ghosts);
 /* GridSolver:boundary() (gridsolver.lua:1316). */
@@ -229,6 +263,9 @@ int hc_batch_destroy(hc_batch* b);
  * every hc_batch_step until t >= t_end or max_steps updates. */
 int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout,
                    double t_end, long long max_steps, unsigned long long tag, int* slot);
+/* hc_batch_admit with the initial condition built on the device. */
+int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* init,
+                        double t_end, long long max_steps, unsigned long long tag, int* slot);
 /* Advances every live instance by up to `steps` updates (each instance with its
  * own CFL dt), in batched launches.  *n_active = instances still stepping. */
 int hc_batch_step(hc_batch* b, int steps, int* n_active);

@@ -36,7 +36,7 @@ def test_struct_layouts_match_header(tmp_path):
     import subprocess
     import hydrocuda
     structs = {"hc_solver_desc": hydrocuda.SolverDesc, "hc_batch_desc": hydrocuda.BatchDesc,
-               "hc_done": hydrocuda.Done, "hc_batch_stats": hydrocuda.BatchStats}
+               "hc_done": hydrocuda.Done, "hc_batch_stats": hydrocuda.BatchStats, "hc_init": hydrocuda.Init}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hydrocuda.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append('printf("%%s %%zu\\n", "%s", sizeof(%s));' % (cname, cname))
@@ -77,3 +77,16 @@ def test_descriptor_mapping_follows_reference_names():
         hydrocuda.make_desc(dict(dim=1, gridSize=8, fluxLimiter="no such limiter"))
     with pytest.raises(ValueError):
         hydrocuda.make_desc(dict(dim=1, gridSize=8, flux="hll"))
+
+
+def test_init_defaults_without_a_device():
+    """hc_init_defaults is host-only: the reference's default states, no device needed."""
+    import hydrocuda
+    L = hydrocuda.load_library()
+    ic = hydrocuda.Init()
+    assert L.hc_init_defaults(0, ctypes.byref(ic)) == 0
+    assert (ic.kind, list(ic.p[:4])) == (0, [1.0, 1.0, 0.125, 0.1])
+    assert L.hc_init_defaults(3, ctypes.byref(ic)) == 0 and ic.seed == 2 and ic.p[0] == 0.01
+    assert L.hc_init_defaults(7, ctypes.byref(ic)) == -1
+    q = hydrocuda.make_init("quadrant", q=[(1, 2, 3, 4)] * 4)
+    assert list(q.p) == [1, 2, 3, 4] * 4

@@ -144,27 +144,64 @@ def test_nonfinite_request_is_contained(hc, ctx):
     np.testing.assert_array_equal(events["state"], ref)
 
 
-def test_autotune_keeps_results(hc, ctx, tmp_path):
-    """Tile shape changes the schedule, not the arithmetic: results stay bit-identical."""
-    probs = [quad(hc, n, s) for n, s in ((150, 21), (90, 22))]
-    outs = []
-    for tune in (False, True):
-        b = hc.Batch(ctx, precision="f32", max_slots=4, **SCHEME)
+def _variants_from_log(path):
+    """(key, [variants]) from an autotune cache file's timing log."""
+    key, vs = None, []
+    for line in open(path):
+        parts = line.split()
+        if len(parts) > 3 and parts[0] == "#" and parts[2] == "variant":
+            key = parts[1]
+            vs.append(int(parts[3]))
+    return key, vs
+
+
+def _solve_all(hc, ctx, probs, scheme, t_end, cache=None):
+    b = hc.Batch(ctx, precision="f32", max_slots=4, **scheme)
+    try:
         for k, (args, cons) in enumerate(probs):
-            b.admit(args, cons, .03, tag=k)
-        if tune:
-            cache = str(tmp_path / "tune.txt")
+            b.admit(args, cons, t_end, tag=k)
+        if cache:
             b.autotune(cache)
-            assert open(cache).read().strip()
-            b.autotune(cache)      # second call reads the cache
         got = {}
-        while len(got) < 2:
+        while len(got) < len(probs):
             b.step(4)
             for ev in b.poll():
                 got[ev["tag"]] = b.fetch(ev["slot"])
-        outs.append(got)
-    for k in range(2):
-        np.testing.assert_array_equal(outs[0][k], outs[1][k])
+        return got, b.stats()["tile"]
+    finally:
+        b.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_every_schedule_same_bits(hc, ctx, tmp_path, dim):
+    """Tile shape, segment length and unrolling change the schedule, not the
+    arithmetic: every compiled schedule of the FP32 stage kernel gives the same
+    bits.  The autotuner times them all once; each is then forced in turn
+    through the tuner's cache file."""
+    if dim == 2:
+        probs = [quad(hc, n, s) for n, s in ((150, 21), (90, 22))]
+        scheme, t_end = SCHEME, .03
+    else:
+        args = cases.c3_blast(28)
+        probs = [(args, hc.blast_state(args))]
+        scheme = dict(usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2")
+        t_end = .02
+    base, _ = _solve_all(hc, ctx, probs, scheme, t_end)
+    cache = str(tmp_path / "tune.txt")
+    tuned, _ = _solve_all(hc, ctx, probs, scheme, t_end, cache)
+    key, variants = _variants_from_log(cache)
+    assert key and len(variants) >= 2
+    for k in range(len(probs)):
+        np.testing.assert_array_equal(tuned[k], base[k])
+    tiles = set()
+    for v in variants:
+        with open(cache, "w") as f:
+            f.write("%s %d\n" % (key, v))
+        got, tile = _solve_all(hc, ctx, probs, scheme, t_end, cache)
+        tiles.add(tuple(tile[dim - 1]))
+        for k in range(len(probs)):
+            np.testing.assert_array_equal(got[k], base[k], err_msg="variant %d" % v)
+    assert len(tiles) >= 2       # the cache file did select other tile shapes
 
 
 def test_served_stream_results_match_alone(hc, ctx):

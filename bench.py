@@ -243,6 +243,8 @@ def main():
                     help="c4: the batched quadrants (the headline); c1 Sod; c2 Kelvin-Helmholtz 1024^2; "
                          "c3 blast 256^3; c5 serving")
     ap.add_argument("--size", type=int, default=0, help="c2 / c3: grid side (default: the configuration's)")
+    ap.add_argument("--schedule", type=int, default=-1,
+                    help="c4: pin the 2D stage-kernel schedule (autotuner variant number) instead of tuning")
     ap.add_argument("--requests", type=int, default=1000,
                     help="c5: requests in the stream (the configuration has 20000)")
     ap.add_argument("--host-states", action="store_true",
@@ -273,7 +275,9 @@ def main():
     b = hc.Batch(ctx, precision="f32", max_slots=len(work), **SCHEME)
     for k, ((a, _), u) in enumerate(zip(work, inputs)):
         b.admit(a, u, t_end=math.inf, tag=k, layout="soa5_f32")
-    if not args.no_autotune:
+    if args.schedule >= 0:
+        b.set_schedule(2, args.schedule)
+    elif not args.no_autotune:
         b.autotune(os.path.join(PKG, "_build", "autotune.txt"))
     st = b.stats()
     b.step(args.warmup)
@@ -401,8 +405,30 @@ def fp64_run(hc, ctx, work):
     _, ms = b.step_timed(3)
     fused = allcells * 3 / (ms / 1e3)
     b.close()
+    # FP32 against FP64 over the configuration's 200 updates, on the first
+    # instances of the workload (both batched)
+    l1, cells_l1 = [], 0
+    got = {}
+    for prec in ("f32", "f64"):
+        bb = hc.Batch(ctx, precision=prec, max_slots=16, **SCHEME)
+        for k, (a, q) in enumerate(work[:16]):
+            bb.admit(a, hc.quadrant_state(a, q), t_end=math.inf, max_steps=E2E_STEPS, tag=k)
+        out = {}
+        while len(out) < min(16, len(work)):
+            bb.step(50)
+            for ev in bb.poll():
+                out[ev["tag"]] = bb.fetch(ev["slot"])
+        bb.close()
+        got[prec] = out
+    for k in got["f32"]:
+        l1.append(float(np.mean(np.abs(got["f32"][k][:, 0] - got["f64"][k][:, 0]))))
+        cells_l1 += got["f32"][k].shape[0]
     return {"plain_value": plain, "plain_sample": "%d grids x 3 updates" % len(sample),
-            "fused_batched_value": fused, "unit": UNIT}
+            "fused_batched_value": fused, "unit": UNIT,
+            "l1_rho_f32_vs_f64": {"max": max(l1), "mean": float(np.mean(l1)),
+                                  "sample": "first %d instances (%d cells), %d updates each, FP64 fused batch as the "
+                                            "FP64 reference (bit-identical to the oracle in the parity tests)" % (
+                                                len(l1), cells_l1, E2E_STEPS)}}
 
 
 # ---------------------------------------------------------------------------
@@ -434,7 +460,7 @@ def _cells(args):
 
 
 def _scheme(args):
-    return {k: args[k] for k in ("usePLM", "slopeLimiter", "fluxLimiter", "integrator") if k in args}
+    return {k: args[k] for k in ("usePLM", "slopeLimiter", "fluxLimiter", "integrator", "flux") if k in args}
 
 
 def l1_density(a, b):
@@ -442,11 +468,12 @@ def l1_density(a, b):
     return float(np.mean(np.abs(a[:, 0] - b[:, 0])))
 
 
-def batch_solve(hc, ctx, args, cons, precision, t_end=math.inf, max_steps=0, chunk=16, init=None):
+def batch_solve(hc, ctx, args, cons, precision, t_end=math.inf, max_steps=0, chunk=16, init=None, checkpoints=()):
     """One solve through the batch API, device-timed stage by stage.  Runs
     until the instance reports done (t >= t_end or max_steps updates).
     Returns the final AoS-6 interior state, updates done, device ms and the
-    Kahan FP64 sums of the conserved fields before and after."""
+    Kahan FP64 sums of the conserved fields before and after; with
+    `checkpoints` (update counts) also the state after each of them."""
     b = hc.Batch(ctx, precision=precision, max_slots=1, **_scheme(args))
     try:
         if init is not None:
@@ -456,6 +483,14 @@ def batch_solve(hc, ctx, args, cons, precision, t_end=math.inf, max_steps=0, chu
         sums0 = b.conservation(slot)
         total_ms = 0.0
         ev = []
+        snaps = {}
+        done = 0
+        for cp in checkpoints:
+            if cp > done:
+                _, ms = b.step_timed(cp - done)
+                total_ms += ms
+                done = cp
+            snaps[cp] = b.fetch(slot, "aos6")
         while not ev:
             n = chunk if not max_steps else max(1, min(chunk, max_steps))
             _, ms = b.step_timed(n)
@@ -464,7 +499,7 @@ def batch_solve(hc, ctx, args, cons, precision, t_end=math.inf, max_steps=0, chu
         state = b.fetch(slot, "aos6")
         sums1 = b.conservation(slot)
         return dict(state=state, steps=ev[0]["steps"], t=ev[0]["t"], ms=total_ms, status=ev[0]["status"],
-                    sums0=sums0, sums1=sums1)
+                    sums0=sums0, sums1=sums1, snaps=snaps)
     finally:
         b.close()
 
@@ -572,7 +607,7 @@ def run_c1(args):
                            "note": "launch-bound at this size; this configuration is the parity case"})
 
 
-def run_grid_config(name, a, U0, t_end, max_steps, plain_updates, oracle_updates):
+def run_grid_config(name, a, U0, t_end, max_steps, plain_updates, oracle_updates, checkpoints=()):
     import hydrocuda as hc
     ctx = hc.Context(0)
     small = dict(a, gridSize=[min(n, 32) for n in a["gridSize"]])
@@ -581,8 +616,8 @@ def run_grid_config(name, a, U0, t_end, max_steps, plain_updates, oracle_updates
         if U_small is None:
             U_small = initial_for(hc, small)
         warm(hc, ctx, small, U_small, prec)
-    r32 = batch_solve(hc, ctx, a, U0, "f32", t_end=t_end, max_steps=max_steps)
-    r64 = batch_solve(hc, ctx, a, U0, "f64", t_end=t_end, max_steps=max_steps)
+    r32 = batch_solve(hc, ctx, a, U0, "f32", t_end=t_end, max_steps=max_steps, checkpoints=checkpoints)
+    r64 = batch_solve(hc, ctx, a, U0, "f64", t_end=t_end, max_steps=max_steps, checkpoints=checkpoints)
     cells = _cells(a)
     v32 = cells * r32["steps"] / (r32["ms"] / 1e3)
     v64 = cells * r64["steps"] / (r64["ms"] / 1e3)
@@ -598,6 +633,7 @@ def run_grid_config(name, a, U0, t_end, max_steps, plain_updates, oracle_updates
                      "peak_kind": peak_kind, "traffic": None,
                      "note": "algorithmic bytes: %d state arrays x 5 fields x 4 B per cell-update" % arrays},
         "l1_rho_f32_vs_f64": l1_density(r32["state"], r64["state"]),
+        "l1_rho_f32_vs_f64_by_step": {str(k): l1_density(r32["snaps"][k], r64["snaps"][k]) for k in checkpoints},
         "fp64": {"fused_value": v64, "plain_value": plain_rate(hc, ctx, a, U0, plain_updates),
                  "plain_sample": "%d updates" % plain_updates,
                  "fused_first_update_max_abs_diff_vs_oracle": fp64_first_update_vs_oracle(hc, ctx, a, U0)},
@@ -623,7 +659,8 @@ def run_c2(args):
     import hydrocuda as hc
     a = conf_kh(args.size or 1024)
     return run_grid_config("2D Kelvin-Helmholtz %d^2, plm cons + MC, Roe, RK3-TVD, CFL .4, periodic, 500 steps"
-                           % a["gridSize"][0], a, hc.kelvin_helmholtz_state(a, seed=2), math.inf, 500, 10, 2)
+                           % a["gridSize"][0], a, hc.kelvin_helmholtz_state(a, seed=2), math.inf, 500, 10, 2,
+                           checkpoints=(1, 10, 50, 100, 200, 300, 400))
 
 
 def run_c3(args):
@@ -720,6 +757,19 @@ def run_c5(args):
             continue
         f64 = batch_solve(hc, ctx, dict(a, **scheme), None, "f64", t_end=t_end, init=init)["state"]
         l1.append(l1_density(r.result, f64))
+    # requests that ended non-finite: the same solve alone in FP32 and in FP64
+    failed = []
+    by_req = {r.tag: r for r in f64_stream}
+    for r in done:
+        if not r.status:
+            continue
+        q = by_req[r.tag]
+        info = {"tag": r.tag, "dim": q.args["dim"], "n": q.args["gridSize"][0], "init": q.init[0],
+                "t_end": q.t_end, "steps": r.steps, "t": r.t}
+        for prec in ("f32", "f64"):
+            rr = batch_solve(hc, ctx, dict(q.args, **scheme), None, prec, t_end=q.t_end, init=q.init)
+            info[prec + "_alone"] = {"status": rr["status"], "steps": rr["steps"]}
+        failed.append(info)
     peaks, peak_kind = measured_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
     gbs = value * 5 * FIELDS * BYTES_PER_VALUE / 1e9
@@ -733,6 +783,7 @@ def run_c5(args):
             "dtype": "f32", "requests": len(reqs), "finished": len(done), "wall_s": wall,
             "requests_per_s": len(done) / wall, "latency": lat,
             "statuses_nonzero": sum(1 for r in done if r.status),
+            "nonfinite_requests": failed,
             "ticks": srv.ticks, "dims": dims,
             "initial_states": "built on the device at admission (hc_batch_admit_init)" if device_init else
                               "built on the host by worker threads, uploaded at admission",

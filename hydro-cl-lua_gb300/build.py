@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + CSRC, "-I" + INCLUDE,
           "--expt-relaxed-constexpr"]
 EXACT = ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"]
-FAST = ["-use_fast_math"]
+FAST = ["-use_fast_math", "-ftz=false"]
 
 SOURCES = {
     "hc_api.cu": [],
@@ -34,6 +34,8 @@ SOURCES = {
     "hc_fused_f32_d2b.cu": FAST,
     "hc_fused_f32_d2c.cu": FAST,
     "hc_fused_f32_d2d.cu": FAST,
+    "hc_fused_f32_flux.cu": FAST,
+    "hc_fused_f32_recon.cu": FAST,
     "hc_fused_f32_d3.cu": FAST,
     "hc_fused_f64_d1.cu": EXACT,
     "hc_fused_f64_d2.cu": EXACT,

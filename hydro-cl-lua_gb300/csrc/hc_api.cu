@@ -87,11 +87,13 @@ int validate_desc(const hc_solver_desc* d) {
             return fail(HC_ERR_INVALID, "unknown boundary");
     if (d->flux_limiter < 0 || d->flux_limiter >= HC_NUM_LIMITERS) return fail(HC_ERR_INVALID, "unknown flux limiter");
     if (d->slope_limiter < 0 || d->slope_limiter >= HC_NUM_LIMITERS) return fail(HC_ERR_INVALID, "unknown slope limiter");
-    if (d->recon < HC_RECON_NONE || d->recon > HC_RECON_PLM_CONS) return fail(HC_ERR_INVALID, "unknown usePLM");
+    if (d->recon < HC_RECON_NONE || d->recon >= HC_NUM_RECONS) return fail(HC_ERR_INVALID, "unknown usePLM");
     if (d->recon != HC_RECON_NONE && d->flux_limiter > 0)
         return fail(HC_ERR_INVALID, "usePLM together with a flux limiter (gridsolver.lua:119 asserts against it)");
     if (d->integrator < 0 || d->integrator >= HC_NUM_INTEGRATORS) return fail(HC_ERR_INVALID, "unknown integrator");
     if (d->precision < HC_F64_PLAIN || d->precision > HC_F32_FUSED) return fail(HC_ERR_INVALID, "unknown precision");
+    if (d->flux < 0 || d->flux >= HC_NUM_FLUXES) return fail(HC_ERR_INVALID, "unknown flux");
+    if (d->hllc_method < HC_HLLC_DEFAULT || d->hllc_method > HC_HLLC_METHOD_2) return fail(HC_ERR_INVALID, "unknown hllcMethod");
     if (!(d->gamma > 1.)) return fail(HC_ERR_INVALID, "gamma must exceed 1");
     if (!(d->cfl > 0.) && !(d->fixed_dt > 0.)) return fail(HC_ERR_INVALID, "cfl must be positive");
     return HC_OK;
@@ -110,6 +112,8 @@ FusedScheme scheme_of(const hc_solver_desc& d) {
     s.recon = d.recon;
     s.slope_limiter = d.slope_limiter;
     s.integrator = d.integrator;
+    s.flux = d.flux;
+    s.hllc_method = d.hllc_method;
     return s;
 }
 
@@ -449,6 +453,11 @@ int hc_batch_create(hc_context* ctx, const hc_batch_desc* desc, hc_batch** out) 
     sch.recon = desc->recon;
     sch.slope_limiter = desc->slope_limiter;
     sch.integrator = desc->integrator;
+    sch.flux = desc->flux;
+    sch.hllc_method = desc->hllc_method;
+    if (desc->flux < 0 || desc->flux >= HC_NUM_FLUXES) return fail(HC_ERR_INVALID, "unknown flux");
+    if (desc->hllc_method < HC_HLLC_DEFAULT || desc->hllc_method > HC_HLLC_METHOD_2)
+        return fail(HC_ERR_INVALID, "unknown hllcMethod");
     hc_batch* b = new hc_batch();
     b->ctx = ctx;
     b->d = *desc;
@@ -479,7 +488,7 @@ static int batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons
     HC_CHECK(validate_desc(desc));
     if (init) HC_CHECK(init_validate(*init, *desc));
     if (desc->recon != b->d.recon || desc->slope_limiter != b->d.slope_limiter || desc->flux_limiter != b->d.flux_limiter ||
-        desc->integrator != b->d.integrator)
+        desc->integrator != b->d.integrator || desc->flux != b->d.flux || desc->hllc_method != b->d.hllc_method)
         return fail(HC_ERR_INVALID, "the instance's scheme differs from the batch's");
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
     if (max_steps <= 0) max_steps = LLONG_MAX;
@@ -590,6 +599,13 @@ int hc_batch_autotune(hc_batch* b, const char* cache_path) {
     if (!b) return fail(HC_ERR_INVALID, "NULL batch");
     HC_CHECK(use_device(b->ctx));
     return fused_autotune(b->fused, cache_path);
+}
+
+int hc_batch_set_schedule(hc_batch* b, int dim, int variant) {
+    if (!b) return fail(HC_ERR_INVALID, "NULL batch");
+    if (dim < 1 || dim > 3) return fail(HC_ERR_INVALID, "dim must be 1, 2 or 3");
+    HC_CHECK(use_device(b->ctx));
+    return fused_set_schedule(b->fused, dim, variant);
 }
 
 }  // extern "C"

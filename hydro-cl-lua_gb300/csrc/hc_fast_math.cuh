@@ -83,6 +83,7 @@ __device__ __forceinline__ T limiter(int which, T r) {
 template <typename T> struct Eos {
     T gamma, g1, rhoMin, PMin;
     int fluxLimiter, slopeLimiter;
+    int hllcMethod;
 };
 
 // A conserved state in the interface frame: rho, m_n, m_t1, m_t2, ETotal.
@@ -207,51 +208,45 @@ __device__ __forceinline__ void makeIface(IfaceF<T>& I, const Eos<T>& s, const C
     left(I.dW, I.e, s, dU);
 }
 
-// Roe flux (roe.cl:17-163) at interface C; IL / IR are the neighbouring
-// interfaces (used only with the flux limiter).
-template <typename T, bool LIM>
-__device__ __forceinline__ void roe(T* F, const Eos<T>& s, const C5<T>& UL, const C5<T>& UR,
-                                    const IfaceF<T>& C, const IfaceF<T>& IL, const IfaceF<T>& IR, T dt_dx) {
-    T UA[5];
-    for (int j = 0; j < 5; ++j) UA[j] = T(.5) * (UL.u[j] + UR.u[j]);
+// fluxFromCons (euler.cl:271-291) in the interface frame:
+// (rho v_n, m_n v_n + P, m_t1 v_n, m_t2 v_n, (ETotal + P) v_n).
+template <typename T>
+__device__ __forceinline__ void fluxOf(T* F, const Eos<T>& s, const C5<T>& U) {
+    T inv, P;
+    primOf(U, s, inv, P);
+    T const vn = U.u[1] * inv;
+    F[0] = U.u[0] * vn;
+    F[1] = U.u[1] * vn + P;
+    F[2] = U.u[2] * vn;
+    F[3] = U.u[3] * vn;
+    F[4] = (U.u[4] + P) * vn;
+}
+
+// Roe flux with the flux limiter (roe.cl:17-163, in the fluxFromCons form
+// Euler inherits, eqn.lua:46) at interface C; IL / IR are the neighbouring
+// interfaces:  F = R.fe + (F(UL) + F(UR)) / 2,
+// fe_j = -lambda_j dW_j (sgn + phi (lambda_j dt/dx - sgn)) / 2.
+template <typename T>
+__device__ __forceinline__ void roeLimited(T* F, const Eos<T>& s, const C5<T>& UL, const C5<T>& UR,
+                                           const IfaceF<T>& C, const IfaceF<T>& IL, const IfaceF<T>& IR, T dt_dx) {
     T fe[5];
-    left(fe, C.e, s, UA);
     T const vn = C.e.vn, Cs = C.e.Cs;
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
         T const lambda = j == 0 ? vn - Cs : (j == 4 ? vn + Cs : vn);
         T const sgn = lambda >= T(0) ? T(1) : T(-1);
-        if (LIM) {
-            T rEig;
-            if (C.dW[j] == T(0)) rEig = T(0);
-            else rEig = M<T>::div(lambda >= T(0) ? IL.dW[j] : IR.dW[j], C.dW[j]);
-            T const phi = limiter<T>(s.fluxLimiter, rEig);
-            fe[j] = fe[j] * lambda - T(.5) * lambda * C.dW[j] * (sgn + phi * (lambda * dt_dx - sgn));
-        } else {
-            fe[j] = fe[j] * lambda - T(.5) * lambda * C.dW[j] * sgn;
-        }
+        T rEig;
+        if (C.dW[j] == T(0)) rEig = T(0);
+        else rEig = M<T>::div(lambda >= T(0) ? IL.dW[j] : IR.dW[j], C.dW[j]);
+        T const phi = limiter<T>(s.fluxLimiter, rEig);
+        fe[j] = T(-.5) * lambda * C.dW[j] * (sgn + phi * (lambda * dt_dx - sgn));
     }
     right(F, C.e, fe);
-}
-
-// Roe flux without the flux limiter, from the two one-sided projections:
-// with sgn(lambda) lambda = |lambda|, the reference's
-//   lambda L.(UL+UR)/2 - |lambda| L.(UR-UL)/2
-// equals max(lambda, 0) L.UL + min(lambda, 0) L.UR component by component.
-template <typename T>
-__device__ __forceinline__ void roeSplit(T* F, const Eos<T>& s, const C5<T>& UL, const C5<T>& UR) {
-    EigF<T> e;
-    eigen(e, s, UL, UR);
-    T wL[5], wR[5], fe[5];
-    left(wL, e, s, UL.u);
-    left(wR, e, s, UR.u);
-    T const lam[3] = {e.vn - e.Cs, e.vn, e.vn + e.Cs};
+    T FL[5], FR[5];
+    fluxOf(FL, s, UL);
+    fluxOf(FR, s, UR);
 #pragma unroll
-    for (int j = 0; j < 5; ++j) {
-        T const l = lam[j == 0 ? 0 : (j == 4 ? 2 : 1)];
-        fe[j] = fmaxf(l, T(0)) * wL[j] + fminf(l, T(0)) * wR[j];
-    }
-    right(F, e, fe);
+    for (int j = 0; j < 5; ++j) F[j] = F[j] + T(.5) * (FL[j] + FR[j]);
 }
 
 // "plm cons" slope of one component: returns sigma.

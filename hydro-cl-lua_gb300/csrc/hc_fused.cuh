@@ -126,6 +126,9 @@ struct StageArgs {
     StageDev st;
     int rot_buf;                // result buffer of a rotating plan (0: the plan does not rotate)
     int* err;
+    int flux;                   // HC_FLUX_*
+    int hllcMethod;             // euler-hllc's hllcMethod, 0..2
+    int recon;                  // HC_RECON_*
 };
 
 // A slot whose step count left its state in the other buffer of a rotating
@@ -229,7 +232,8 @@ struct TileK {
 // per-step coefficients: loads only, no FP64 arithmetic in the stage kernel.
 template <typename T>
 __device__ __forceinline__ void makeTileK(TileK<T>& k, const DevInst& I, const DevCtl* c, const StageDev* st,
-                                          int slopeLim, int fluxLim) {
+                                          int slopeLim, int fluxLim, int flux = HC_FLUX_ROE, int hllcMethod = 2,
+                                          int recon = HC_RECON_NONE) {
     if constexpr (sizeof(T) == 4) {
         k.fe.gamma = I.f_gamma;
         k.fe.g1 = I.f_g1;
@@ -250,6 +254,10 @@ __device__ __forceinline__ void makeTileK(TileK<T>& k, const DevInst& I, const D
     k.re.PMin = I.PMin;
     k.re.fluxLimiter = fluxLim;
     k.re.slopeLimiter = slopeLim;
+    k.re.flux = flux;
+    k.re.hllcMethod = hllcMethod;
+    k.re.recon = recon;
+    k.fe.hllcMethod = hllcMethod;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         if constexpr (sizeof(T) == 4) {
@@ -389,7 +397,7 @@ struct BoxGeom {
 // UNR: unroll factor of the sliding-window loop (0: fully unrolled).  Full
 // unrolling removes the window copies; partial unrolling keeps the code
 // footprint inside the instruction cache.
-template <typename T, int AXIS, int STRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, int SLOPE, int UNR, class Emit>
+template <typename T, int AXIS, int STRIDE, int BOXN, int L, bool EXACT, int PLM, bool LIM, int SLOPE, int UNR, class Emit>
 __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK<T>& K, Emit&& emit) {
     // SLOPE >= 0 fixes the slope limiter at compile time; -1 dispatches at run time
     int const slopeLim = SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter;
@@ -406,15 +414,26 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
         auto flux = [&](double* out, const double* UL, const double* UR, const ref::Iface& C,
                         const ref::Iface* IL, const ref::Iface* IR) {
             if (zero) { for (int j = 0; j < 6; ++j) out[j] = 0.; return; }
-            ref::roeFlux(out, e, UL, UR, C, IL, IR, AXIS, LIM, dt_dx);
+            if (e.flux == HC_FLUX_RUSANOV) {
+                ref::rusanovFlux(out, e, UL, UR, AXIS);
+            } else if (e.flux == HC_FLUX_HLL || e.flux == HC_FLUX_HLLC) {
+                // a NaN wave bound assigns nothing in the reference (its flux
+                // buffer keeps stale values); this form has no flux buffer
+                bool const set = e.flux == HC_FLUX_HLL ? ref::hllFlux(out, e, UL, UR, AXIS, C.eig)
+                                                       : ref::hllcFlux(out, e, UL, UR, AXIS, C.eig);
+                if (!set)
+                    for (int j = 0; j < 6; ++j) out[j] = __longlong_as_double(0x7ff8000000000000ll);
+            } else {
+                ref::roeFlux(out, e, UL, UR, C, IL, IR, AXIS, LIM, dt_dx);
+            }
         };
-        if constexpr (PLM) {
+        if constexpr (PLM != 0) {
             double Um[6], U0[6], Up[6], prevR[6], fL[6], fR[6];
             load(-2, Um);
             load(-1, U0);
             for (int k = -1; k <= L; ++k) {
                 load(k + 1, Up);
-                ref::plmCons(fL, fR, e, Um, U0, Up);
+                ref::plmAny(fL, fR, e, Um, U0, Up, AXIS);
                 if (k >= 0) {
                     ref::Iface C;
                     ref::makeIface(C, e, prevR, fL, AXIS);
@@ -454,6 +473,8 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
             }
         }
     } else {
+        // the fast form with the flux limiter (the others run sweepLanes)
+        static_assert(LIM && PLM == 0, "the fast form sweeps here only with the flux limiter");
         using C5 = fast::C5<T>;
         fast::Eos<T> const& e = K.fe;
         T const dt_dx = K.dtdx[AXIS];
@@ -468,94 +489,33 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
             U.u[4] = box[4 * BOXN + i];
         };
         bool const zero = K.zero[AXIS];
-        // flux in the interface frame, then back to the global frame
         T Fprev[5], F[5];
-        auto flux = [&](T* out, const C5& UL, const C5& UR, const fast::IfaceF<T>& C,
-                        const fast::IfaceF<T>& IL, const fast::IfaceF<T>& IR) {
-            T Fr[5];
-            fast::roe<T, LIM>(Fr, e, UL, UR, C, IL, IR, dt_dx);
-            if (zero) for (int j = 0; j < 5; ++j) Fr[j] = T(0);
-            out[0] = Fr[0];
-            out[A1] = Fr[1];
-            out[A2] = Fr[2];
-            out[A3] = Fr[3];
-            out[4] = Fr[4];
-        };
-        if constexpr (PLM) {
-            C5 Um, U0, Up, prevR, fL, fR;
-            T dL[5];     // U0 - Um, carried from the previous cell's right difference
-            load(-2, Um);
-            load(-1, U0);
-#pragma unroll
-            for (int j = 0; j < 5; ++j) dL[j] = U0.u[j] - Um.u[j];
-#pragma unroll (UNR == 0 ? L + 2 : UNR)
-            for (int k = -1; k <= L; ++k) {
-                load(k + 1, Up);
-#pragma unroll
-                for (int j = 0; j < 5; ++j) {
-                    T const dR = Up.u[j] - U0.u[j];
-                    T const sg = fast::plmHalfSlopeD<T, SLOPE>(dL[j], dR, slopeLim);
-                    fL.u[j] = U0.u[j] - sg;
-                    fR.u[j] = U0.u[j] + sg;
-                    dL[j] = dR;
-                }
-                if (k >= 0) {
-                    T Fr[5];
-                    fast::roeSplit<T>(Fr, e, prevR, fL);
-                    if (zero) for (int j = 0; j < 5; ++j) Fr[j] = T(0);
-                    F[0] = Fr[0];
-                    F[A1] = Fr[1];
-                    F[A2] = Fr[2];
-                    F[A3] = Fr[3];
-                    F[4] = Fr[4];
-                    if (k >= 1) emit(k - 1, Fprev, F);
-#pragma unroll
-                    for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
-                }
-                prevR = fR;
-                Um = U0;
-                U0 = Up;
-            }
-        } else if constexpr (LIM) {
-            C5 Ua, Ub, Uc, Ud;
-            fast::IfaceF<T> IL, IC, IR;
-            load(-2, Ua);
-            load(-1, Ub);
-            load(0, Uc);
-            fast::makeIface(IL, e, Ua, Ub);
-            fast::makeIface(IC, e, Ub, Uc);
+        C5 Ua, Ub, Uc, Ud;
+        fast::IfaceF<T> IL, IC, IR;
+        load(-2, Ua);
+        load(-1, Ub);
+        load(0, Uc);
+        fast::makeIface(IL, e, Ua, Ub);
+        fast::makeIface(IC, e, Ub, Uc);
 #pragma unroll 1
-            for (int k = 0; k <= L; ++k) {
-                load(k + 1, Ud);
-                fast::makeIface(IR, e, Uc, Ud);
-                flux(F, Ub, Uc, IC, IL, IR);
-                if (k >= 1) emit(k - 1, Fprev, F);
+        for (int k = 0; k <= L; ++k) {
+            load(k + 1, Ud);
+            fast::makeIface(IR, e, Uc, Ud);
+            T Fr[5];
+            fast::roeLimited<T>(Fr, e, Ub, Uc, IC, IL, IR, dt_dx);
+            if (zero) for (int j = 0; j < 5; ++j) Fr[j] = T(0);
+            F[0] = Fr[0];
+            F[A1] = Fr[1];
+            F[A2] = Fr[2];
+            F[A3] = Fr[3];
+            F[4] = Fr[4];
+            if (k >= 1) emit(k - 1, Fprev, F);
 #pragma unroll
-                for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
-                Ub = Uc;
-                Uc = Ud;
-                IL = IC;
-                IC = IR;
-            }
-        } else {
-            C5 Ua, Ub;
-            load(-1, Ua);
-#pragma unroll (UNR == 0 ? L + 1 : UNR)
-            for (int k = 0; k <= L; ++k) {
-                load(k, Ub);
-                T Fr[5];
-                fast::roeSplit<T>(Fr, e, Ua, Ub);
-                if (zero) for (int j = 0; j < 5; ++j) Fr[j] = T(0);
-                F[0] = Fr[0];
-                F[A1] = Fr[1];
-                F[A2] = Fr[2];
-                F[A3] = Fr[3];
-                F[4] = Fr[4];
-                if (k >= 1) emit(k - 1, Fprev, F);
-#pragma unroll
-                for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
-                Ua = Ub;
-            }
+            for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
+            Ub = Uc;
+            Uc = Ud;
+            IL = IC;
+            IC = IR;
         }
     }
 }
@@ -564,7 +524,8 @@ __device__ __forceinline__ void sweepSegment(const T* box, int base, const TileK
 // at once (fast form, no flux limiter): lane l's line starts at box index
 // base + l * LSTRIDE.  emit(k, FL, FR) receives, for cell k of the segment,
 // the left and right face fluxes of every lane in the global frame.
-template <typename V, int AXIS, int STRIDE, int LSTRIDE, int BOXN, int L, bool PLM, int SLOPE, int UNR, class Emit>
+template <typename V, int AXIS, int STRIDE, int LSTRIDE, int BOXN, int L, int PLM, int SLOPE, int UNR, int FLUX,
+          class Emit>
 __device__ __forceinline__ void sweepLanes(const float* box, int base, const lanes::Eos& e, int slopeLim, bool zero,
                                            Emit&& emit) {
     using C5 = lanes::C5<V>;
@@ -593,7 +554,10 @@ __device__ __forceinline__ void sweepLanes(const float* box, int base, const lan
     V F[5], Fprev[5];
     auto flux = [&](const C5& UL, const C5& UR) {
         V Fr[5];
-        lanes::roeSplit<V>(Fr, e, UL, UR);
+        if constexpr (FLUX == HC_FLUX_HLL) lanes::hll<V>(Fr, e, UL, UR);
+        else if constexpr (FLUX == HC_FLUX_HLLC) lanes::hllc<V>(Fr, e, UL, UR);
+        else if constexpr (FLUX == HC_FLUX_RUSANOV) lanes::rusanov<V>(Fr, e, UL, UR);
+        else lanes::roe<V>(Fr, e, UL, UR);
         if (zero) for (int j = 0; j < 5; ++j) Fr[j] = lanes::splat<V>(0.f);
         F[0] = Fr[0];
         F[A1] = Fr[1];
@@ -601,7 +565,7 @@ __device__ __forceinline__ void sweepLanes(const float* box, int base, const lan
         F[A3] = Fr[3];
         F[4] = Fr[4];
     };
-    if constexpr (PLM) {
+    if constexpr (PLM == HC_RECON_PLM_CONS) {
         C5 Um, U0, Up, prevR, fL, fR;
         V dL[5];
         load(-2, Um);
@@ -629,6 +593,49 @@ __device__ __forceinline__ void sweepLanes(const float* box, int base, const lan
             Um = U0;
             U0 = Up;
         }
+    } else if constexpr (PLM != 0) {
+        // "plm prim" / "plm athena", or (PLM < 0) the reconstruction the
+        // scheme names, chosen at run time; the window keeps each cell's
+        // primitives next to its conserved state
+        C5 Um, U0, Up, prevR, fL, fR;
+        V Wm[5], W0[5], Wp[5];
+        load(-2, Um);
+        lanes::primOf(Wm, e, Um);
+        load(-1, U0);
+        lanes::primOf(W0, e, U0);
+        int const rc = PLM > 0 ? PLM : e.recon;
+#pragma unroll 1
+        for (int k = -1; k <= L; ++k) {
+            load(k + 1, Up);
+            lanes::primOf(Wp, e, Up);
+            if (rc == HC_RECON_PLM_ATHENA) {
+                lanes::plmAthena<V>(fL, fR, e, U0, Wm, W0, Wp);
+            } else if (rc == HC_RECON_PLM_PRIM) {
+                lanes::plmPrim<V>(fL, fR, e, Wm, W0, Wp, slopeLim);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 5; ++j) {
+                    V const h = lanes::halfSlope<SLOPE>(lanes::sub(U0.u[j], Um.u[j]), lanes::sub(Up.u[j], U0.u[j]),
+                                                        slopeLim);
+                    fL.u[j] = lanes::sub(U0.u[j], h);
+                    fR.u[j] = lanes::add(U0.u[j], h);
+                }
+            }
+            if (k >= 0) {
+                flux(prevR, fL);
+                if (k >= 1) emit(k - 1, Fprev, F);
+#pragma unroll
+                for (int j = 0; j < 5; ++j) Fprev[j] = F[j];
+            }
+            prevR = fR;
+            Um = U0;
+            U0 = Up;
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                Wm[j] = W0[j];
+                W0[j] = Wp[j];
+            }
+        }
     } else {
         C5 Ua, Ub;
         load(-1, Ua);
@@ -651,14 +658,14 @@ __device__ __forceinline__ float laneOf(float2 v, int k) { return k ? v.y : v.x;
 // One segment sweep: the FP32 fast form without a flux limiter runs the
 // lane-generic arithmetic (LANES lines at once); the exact form and the
 // flux-limited fast form run sweepSegment (one line).
-template <typename T, int AXIS, int STRIDE, int LSTRIDE, int BOXN, int L, bool EXACT, bool PLM, bool LIM, int SLOPE,
-          int UNR, int LANES, class Emit>
+template <typename T, int AXIS, int STRIDE, int LSTRIDE, int BOXN, int L, bool EXACT, int PLM, bool LIM, int SLOPE,
+          int UNR, int LANES, int FLUX, class Emit>
 __device__ __forceinline__ void sweepAny(const T* box, int base, const TileK<T>& K, Emit&& emit) {
     if constexpr (!EXACT && !LIM && sizeof(T) == 4) {
         using V = typename std::conditional<LANES == 2, float2, float>::type;
-        lanes::Eos const e{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin};
-        sweepLanes<V, AXIS, STRIDE, LSTRIDE, BOXN, L, PLM, SLOPE, UNR>(box, base, e, SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter,
-                                                                      K.zero[AXIS], emit);
+        lanes::Eos const e{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon};
+        sweepLanes<V, AXIS, STRIDE, LSTRIDE, BOXN, L, PLM, SLOPE, UNR, FLUX>(
+            box, base, e, SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter, K.zero[AXIS], emit);
     } else {
         static_assert(LANES == 1, "two-lane sweeps need the FP32 fast form without a flux limiter");
         sweepSegment<T, AXIS, STRIDE, BOXN, L, EXACT, PLM, LIM, SLOPE, UNR>(box, base, K, emit);
@@ -694,8 +701,10 @@ constexpr int residentCtas(int nt, size_t smem) {
     return o > 32 ? 32 : (o < 1 ? 1 : o);
 }
 
-template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM, int SLOPE, int UNR,
-          int OCC, int LANES>
+// FLUX: the interface flux of the fast form (HC_FLUX_*); the exact form
+// reads it from the launch arguments.
+template <typename T, int DIM, int TX, int TY, int TZ, int L, int NT, bool EXACT, int PLM, bool LIM, int SLOPE, int UNR,
+          int OCC, int LANES, int FLUX>
 __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ StageArgs a, int slopeLim, int fluxLim) {
     static_assert(LANES == 1 || (DIM >= 2 && TX % 2 == 0 && TY % 2 == 0), "two-lane sweeps pair rows and columns");
     using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
@@ -734,7 +743,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
         }
         // the tile's constants (loads; no FP64 arithmetic) while the tile streams in
         TileK<T> K;
-        makeTileK<T>(K, I, ctl, &st, slopeLim, fluxLim);
+        makeTileK<T>(K, I, ctl, &st, slopeLim, fluxLim, a.flux, a.hllcMethod, a.recon);
         if (!mbar_wait_bounded(bar, phase, kSpinLimit)) {
             // the copy did not complete: record it, give the copy a second
             // bounded chance to land before the CTA releases its smem, stop
@@ -764,7 +773,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
                         if (x0 + cx0 >= nx || y0 + cy >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + (DIM > 2 ? 2 : 0)) * G::BY + (cy + 2)) * G::BX + (cx0 + 2);
                         T* Dl = D + (cz * TY + cy) * G::DPX + cx0;
-                        sweepAny<T, 0, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES>(box, base, K,
+                        sweepAny<T, 0, 1, G::BX, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES, FLUX>(box, base, K,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                                 for (int l = 0; l < LANES; ++l)
@@ -789,7 +798,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
                         if (x0 + cx >= nx || y0 + cy0 >= ny || z0 + cz >= nz) continue;
                         int const base = ((cz + 2) * G::BY + (cy0 + 2)) * G::BX + (cx + 2);
                         T* Dl = D + (cz * TY + cy0) * G::DPX + cx;
-                        sweepAny<T, 1, G::BX, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES>(box, base, K,
+                        sweepAny<T, 1, G::BX, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES, FLUX>(box, base, K,
                             [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                                 for (int l = 0; l < LANES; ++l)
@@ -874,8 +883,10 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
 
         // the fast form's epilogue, written with the lane operations: V = float
         // finishes the cell (gx, gy, gz); V = float2 finishes it and its +x
-        // neighbour with packed arithmetic and 8-byte loads and stores
-        auto finishFast = [&](auto vtag, int gx, int gy, int gz, int bi, const T* Dc) {
+        // neighbour with packed arithmetic and 8-byte loads and stores, or
+        // only the first when `second` is false (the neighbour is a ghost or
+        // padding cell: loaded and computed, never stored)
+        auto finishFast = [&](auto vtag, int gx, int gy, int gz, int bi, const T* Dc, bool second) {
             using V = decltype(vtag);
             constexpr int NL = lanes::nlanes<V>();
             long long const idx = padIndex<DIM>(I, gx, gy, gz);
@@ -885,9 +896,10 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             };
             auto st_ = [&](T* p, V v) {
                 if constexpr (NL == 1) *p = v;
-                else *reinterpret_cast<float2*>(p) = v;
+                else if (second) *reinterpret_cast<float2*>(p) = v;
+                else *p = lanes::lane(v, 0);
             };
-            lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin};
+            lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon};
             V u[5], deriv[5];
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
@@ -895,19 +907,37 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
                 else deriv[f] = make_float2(Dc[f * G::DN], Dc[f * G::DN + 1]);
                 u[f] = lanes::splat<V>(0.f);
             }
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                if (m >= st.n_alpha) break;
+            // sum alpha_k u^(k) as p + sum_{k < last} alpha_k (u^(k) - p), p the
+            // last alpha term: every integrator's alpha row sums to 1, and in
+            // this form the weights sum to exactly 1 whatever the FP32 rounding
+            // of the alphas (summed directly, RK3-TVD's 1/3 and 2/3 rounded to
+            // FP32 add 3e-8 of every conserved quantity per step)
+            auto ldAlpha = [&](int m, V* v) {
                 int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
-                V const c = lanes::splat<V>(K.calpha[m]);
                 if (b == inBuf) {
 #pragma unroll
-                    for (int f = 0; f < 5; ++f) u[f] = lanes::fma(ld(box + f * G::BOXN + bi), c, u[f]);
+                    for (int f = 0; f < 5; ++f) v[f] = ld(box + f * G::BOXN + bi);
                 } else {
                     const T* src = reinterpret_cast<const T*>(I.buf[b]);
 #pragma unroll
-                    for (int f = 0; f < 5; ++f) u[f] = lanes::fma(ld(src + f * I.plane + idx), c, u[f]);
+                    for (int f = 0; f < 5; ++f) v[f] = ld(src + f * I.plane + idx);
                 }
+            };
+            int const last = st.n_alpha - 1;
+            V p[5];
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+                if (m == last) ldAlpha(m, p);
+#pragma unroll
+            for (int f = 0; f < 5; ++f) u[f] = p[f];
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                if (m >= last) break;
+                V const c = lanes::splat<V>(K.calpha[m]);
+                V w[5];
+                ldAlpha(m, w);
+#pragma unroll
+                for (int f = 0; f < 5; ++f) u[f] = lanes::fma(lanes::sub(w[f], p[f]), c, u[f]);
             }
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
@@ -933,6 +963,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             if (st.last) dtv = lanes::dtCell<V, DIM>(u, le, K.gdx);
 #pragma unroll
             for (int l = 0; l < NL; ++l) {
+                if (l > 0 && !second) break;
                 T uu[5];
 #pragma unroll
                 for (int f = 0; f < 5; ++f) uu[f] = lanes::lane(u[f], l);
@@ -954,7 +985,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             if (gx0 >= nx || gy0 >= ny || gz0 >= nz) continue;
             int const base = ((c0[2] + (DIM > 2 ? 2 : 0)) * G::BY + (c0[1] + (DIM > 1 ? 2 : 0))) * G::BX + (c0[0] + 2);
             T* Dl = D + (c0[2] * TY + c0[1]) * G::DPX + c0[0];
-            sweepAny<T, AX, STRIDE_AX, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES>(box, base, K,
+            sweepAny<T, AX, STRIDE_AX, 1, G::BOXN, L, EXACT, PLM, LIM, SLOPE, UNR, LANES, FLUX>(box, base, K,
                 [&](int k, const auto* FL, const auto* FR) {
 #pragma unroll
                     for (int l = 0; l < LANES; ++l)
@@ -977,14 +1008,16 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
                     finishCell(g[0], g[1], g[2], base + k * STRIDE_AX, Dl + k * DSTRIDE_AX);
                 }
             } else {
-                // LANES = 2: the line pair, unless the second line lies beyond the grid
+                // LANES = 2: the line pair; the second line may lie beyond the grid
                 bool const pair = LANES == 2 && gx0 + 1 < nx;
 #pragma unroll 1
                 for (int k = 0; k < kmax; ++k) {
                     int g[3] = {gx0, gy0, gz0};
                     g[AX] += k;
-                    if (LANES == 2 && pair) finishFast(float2{}, g[0], g[1], g[2], base + k * STRIDE_AX, Dl + k * DSTRIDE_AX);
-                    else finishFast(T{}, g[0], g[1], g[2], base + k * STRIDE_AX, Dl + k * DSTRIDE_AX);
+                    if constexpr (LANES == 2)
+                        finishFast(float2{}, g[0], g[1], g[2], base + k * STRIDE_AX, Dl + k * DSTRIDE_AX, pair);
+                    else
+                        finishFast(T{}, g[0], g[1], g[2], base + k * STRIDE_AX, Dl + k * DSTRIDE_AX, true);
                 }
             }
         }
@@ -1132,12 +1165,14 @@ __global__ void k_sums(const DevInst* inst, int slot, int buf, double vol, doubl
 struct StageLauncher {
     int precision;   // HC_F32_FUSED / HC_F64_FUSED
     int dim;
-    bool plm, lim;
+    int recon;       // HC_RECON_PLM_* compiled in, 0 (none), or -1 (any PLM kind, read at run time)
+    bool lim;
     int slope;       // slope limiter compiled in, or -1 (any, dispatched at run time)
     int variant;     // tile-shape candidate index
     int tx, ty, tz, nthreads;
     int seg, unroll, min_ctas;   // segment length, sliding-window unroll (0: full), CTAs per SM compiled for
     int lanes;                   // lines per thread (2: packed FP32 pairs)
+    int flux;                    // HC_FLUX_* compiled in, or -1 (any: read at run time)
     size_t smem;
     void (*launch)(const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s);
     int (*occupancy)();   // CTAs per SM (sets the smem attribute first); <= 0 on error

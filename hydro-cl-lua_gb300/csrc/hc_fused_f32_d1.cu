@@ -11,8 +11,8 @@ void register_f32_d1(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& a
     // variants: tile 128 x (L 4, 32 threads); tile 64 x (L 2, 32 threads)
     add_plm_set<T, P, 1, 0, 128, 1, 1, 4, 32>(st);
     add_plm_set<T, P, 1, 1, 64, 1, 1, 2, 32>(st);
-    add_stage<T, P, 1, 0, 128, 1, 1, 4, 32, E, false, false>(st);
-    add_stage<T, P, 1, 0, 128, 1, 1, 4, 32, E, false, true>(st);
+    add_stage<T, P, 1, 0, 128, 1, 1, 4, 32, E, 0, false>(st);
+    add_stage<T, P, 1, 0, 128, 1, 1, 4, 32, E, 0, true>(st);
     add_aux<T, P, 1, E>(aux);
 }
 

@@ -9,8 +9,8 @@ void register_f32_d2b(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& 
     using T = float;
     constexpr int P = HC_F32_FUSED;
     constexpr bool E = false;
-    add_stage<T, P, 2, 0, 32, 32, 1, 4, 256, E, false, false>(st);
-    add_stage<T, P, 2, 0, 32, 32, 1, 4, 256, E, false, true>(st);
+    add_stage<T, P, 2, 0, 32, 32, 1, 4, 256, E, 0, false>(st);
+    add_stage<T, P, 2, 0, 32, 32, 1, 4, 256, E, 0, true>(st);
     add_aux<T, P, 2, E>(aux);
 }
 

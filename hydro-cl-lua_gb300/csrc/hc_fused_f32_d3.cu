@@ -13,10 +13,10 @@ void register_f32_d3(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& a
     add_plm_set<T, P, 3, 0, 16, 8, 8, 4, 256>(st);
     add_plm_set<T, P, 3, 1, 32, 8, 8, 8, 256>(st);
     add_plm_pair<T, P, 3, 2, 16, 8, 8, 8, 128, 0>(st);
-    // 3: 16x8x8, segments of 4, 128 threads, two lines per thread (packed FP32 pairs)
-    add_plm_set<T, P, 3, 3, 16, 8, 8, 4, 128, 0, 0, 2>(st);
-    add_stage<T, P, 3, 0, 16, 8, 8, 4, 256, E, false, false>(st);
-    add_stage<T, P, 3, 0, 16, 8, 8, 4, 256, E, false, true>(st);
+    // 3: 16x8x8, segments of 4, 256 threads, 1 CTA per SM (255 registers)
+    add_plm_set<T, P, 3, 3, 16, 8, 8, 4, 256, 0, 1>(st);
+    add_stage<T, P, 3, 0, 16, 8, 8, 4, 256, E, 0, false>(st);
+    add_stage<T, P, 3, 0, 16, 8, 8, 4, 256, E, 0, true>(st);
     add_aux<T, P, 3, E>(aux);
 }
 

@@ -8,9 +8,9 @@ void register_f64_d2(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& a
     using T = double;
     constexpr int P = HC_F64_FUSED;
     constexpr bool E = true;
-    add_stage<T, P, 2, 0, 32, 32, 1, 8, 128, E, true, false>(st);
-    add_stage<T, P, 2, 0, 32, 32, 1, 8, 128, E, false, false>(st);
-    add_stage<T, P, 2, 0, 32, 32, 1, 8, 128, E, false, true>(st);
+    add_stage<T, P, 2, 0, 32, 32, 1, 8, 128, E, -1, false>(st);
+    add_stage<T, P, 2, 0, 32, 32, 1, 8, 128, E, 0, false>(st);
+    add_stage<T, P, 2, 0, 32, 32, 1, 8, 128, E, 0, true>(st);
     add_aux<T, P, 2, E>(aux);
 }
 

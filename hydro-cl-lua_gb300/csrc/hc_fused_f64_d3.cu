@@ -8,9 +8,9 @@ void register_f64_d3(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& a
     using T = double;
     constexpr int P = HC_F64_FUSED;
     constexpr bool E = true;
-    add_stage<T, P, 3, 0, 16, 8, 8, 8, 128, E, true, false>(st);
-    add_stage<T, P, 3, 0, 16, 8, 8, 8, 128, E, false, false>(st);
-    add_stage<T, P, 3, 0, 16, 8, 8, 8, 128, E, false, true>(st);
+    add_stage<T, P, 3, 0, 16, 8, 8, 8, 128, E, -1, false>(st);
+    add_stage<T, P, 3, 0, 16, 8, 8, 8, 128, E, 0, false>(st);
+    add_stage<T, P, 3, 0, 16, 8, 8, 8, 128, E, 0, true>(st);
     add_aux<T, P, 3, E>(aux);
 }
 

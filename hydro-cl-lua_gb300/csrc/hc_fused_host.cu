@@ -138,6 +138,8 @@ const std::vector<AuxLauncher>& aux_launchers() { return registry().aux; }
 
 size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+constexpr int kMaxVariants = 32;   // schedule numbers the autotuner tries
+
 }  // namespace
 
 struct Slot {
@@ -188,15 +190,27 @@ struct FusedSet {
 };
 
 static const StageLauncher* find_launcher(const FusedScheme& sch, int dim, int variant) {
-    bool const plm = sch.recon == HC_RECON_PLM_CONS;
-    bool const lim = sch.flux_limiter > 0;
-    const StageLauncher* generic = nullptr;
+    // the reconstruction a kernel must provide: 0 when the interface states
+    // are the cells themselves (no PLM, or "piecewise constant")
+    int const want = sch.recon >= HC_RECON_PLM_CONS ? sch.recon : 0;
+    // only the Roe flux takes the flux limiter (fvsolver.lua:62-64)
+    bool const lim = sch.flux_limiter > 0 && sch.flux == HC_FLUX_ROE;
+    // prefer the reconstruction compiled in over any-kind (-1), then the
+    // slope limiter compiled in over any (-1)
+    const StageLauncher* best = nullptr;
+    int bestScore = -1;
     for (const StageLauncher& L : stage_launchers()) {
-        if (L.precision != sch.precision || L.dim != dim || L.plm != plm || L.lim != lim || L.variant != variant) continue;
-        if (plm && L.slope == sch.slope_limiter) return &L;    // slope limiter compiled in
-        if (L.slope < 0) generic = &L;
+        if (L.precision != sch.precision || L.dim != dim || L.lim != lim || L.variant != variant) continue;
+        if (L.flux >= 0 && L.flux != sch.flux) continue;
+        if (want == 0 ? L.recon != 0 : (L.recon != want && L.recon != -1)) continue;
+        if (want != 0 && L.slope >= 0 && L.slope != sch.slope_limiter) continue;
+        int const score = (L.recon == want ? 2 : 0) + (L.slope >= 0 ? 1 : 0);
+        if (score > bestScore) {
+            best = &L;
+            bestScore = score;
+        }
     }
-    return generic;
+    return best;
 }
 
 static const AuxLauncher* find_aux(int precision, int dim) {
@@ -625,6 +639,9 @@ static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
             a.nitems = f->d_nitems + d;
             a.err = f->d_err;
             a.rot_buf = f->rot_buf;
+            a.flux = f->sch.flux;
+            a.hllcMethod = f->sch.hllc_method == HC_HLLC_DEFAULT ? 2 : f->sch.hllc_method - 1;
+            a.recon = f->sch.recon;
             fill_stage(a.st, P.stage[s], P.stage[s].index);
             f->launcher[d]->launch(a, f->sch.slope_limiter, f->sch.flux_limiter, f->grid[d], f->stream);
         }
@@ -856,7 +873,7 @@ static std::string tune_key(const FusedSet* f, int dim, long long cells) {
     int bucket = 0;
     while ((1ll << (bucket + 1)) <= cells) ++bucket;
     std::ostringstream o;
-    o << "p" << f->sch.precision << "_d" << dim << "_plm" << (f->sch.recon == HC_RECON_PLM_CONS) << "_lim"
+    o << "p" << f->sch.precision << "_d" << dim << "_plm" << (f->sch.recon >= HC_RECON_PLM_CONS ? f->sch.recon - 1 : 0) << "_lim"
       << (f->sch.flux_limiter > 0) << "_c" << bucket;
     return o.str();
 }
@@ -896,7 +913,7 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
         int best = 0;
         float bestMs = 1e30f;
         std::ostringstream log;
-        for (int v = 0; v < 16; ++v) {
+        for (int v = 0; v < kMaxVariants; ++v) {
             if (!find_launcher(f->sch, dim, v)) continue;
             HC_CHECK(set_launcher(f, dim, v));
             reencode_all(f, dim);
@@ -949,6 +966,16 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
 
 int fused_variant(const FusedSet* f, int dim) { return f->launcher[dim - 1] ? f->launcher[dim - 1]->variant : -1; }
 
+int fused_set_schedule(FusedSet* f, int dim, int variant) {
+    if (!find_launcher(f->sch, dim, variant)) return fail(HC_ERR_INVALID, "no such schedule for this scheme and dimension");
+    HC_CUDA(cudaStreamSynchronize(f->stream));
+    HC_CHECK(set_launcher(f, dim, variant));
+    reencode_all(f, dim);
+    f->items_dirty = true;
+    f->graph_valid = false;
+    return HC_OK;
+}
+
 }  // namespace hc
 
 namespace hc {
@@ -958,6 +985,8 @@ void register_f32_d2a(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2c(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2d(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_flux(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_recon(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -969,6 +998,8 @@ void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>
     register_f32_d2b(st, aux);
     register_f32_d2c(st, aux);
     register_f32_d2d(st, aux);
+    register_f32_flux(st, aux);
+    register_f32_recon(st, aux);
     register_f32_d3(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);

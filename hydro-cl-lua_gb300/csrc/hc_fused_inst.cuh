@@ -11,15 +11,20 @@ namespace fz {
 // OCC: minimum resident CTAs per SM the kernel is compiled for (0: as many as
 // its shared memory and thread count allow).  LANES: lines each thread sweeps
 // at once (2: packed FP32 pairs).
-template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, bool EXACT, bool PLM, bool LIM,
-          int SLOPE = -1, int UNR = 0, int OCC = 0, int LANES = 1>
+// PLM: the reconstruction compiled in (HC_RECON_PLM_CONS / _PRIM / _ATHENA),
+// 0 for none ("piecewise constant" included: it is the cell itself), or -1:
+// any of the three, read from the scheme at run time.
+// FLUX: the fast form's interface flux compiled in (HC_FLUX_*); the exact form
+// dispatches at run time and registers as any flux (-1).
+template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, bool EXACT, int PLM, bool LIM,
+          int SLOPE = -1, int UNR = 0, int OCC = 0, int LANES = 1, int FLUX = HC_FLUX_ROE>
 void add_stage(std::vector<StageLauncher>& v) {
     using Cfg = StageCfg<T, DIM, TX, TY, TZ, L, NT>;
     constexpr int K = OCC > 0 ? OCC : residentCtas(NT, Cfg::SMEM);
     StageLauncher sl;
     sl.precision = PREC;
     sl.dim = DIM;
-    sl.plm = PLM;
+    sl.recon = PLM;
     sl.lim = LIM;
     sl.slope = SLOPE;
     sl.variant = VAR;
@@ -31,12 +36,13 @@ void add_stage(std::vector<StageLauncher>& v) {
     sl.unroll = UNR;
     sl.min_ctas = K;
     sl.lanes = LANES;
+    sl.flux = EXACT ? -1 : FLUX;
     sl.smem = Cfg::SMEM;
     sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
-        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR, K, LANES><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+        k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR, K, LANES, FLUX><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
     };
     sl.occupancy = []() -> int {
-        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR, K, LANES>;
+        auto k = k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR, K, LANES, FLUX>;
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NT, Cfg::SMEM) != cudaSuccess) return -1;
@@ -55,19 +61,19 @@ inline unsigned aux_blocks(long long n) {
 template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, int UNR = 0, int OCC = 0,
           int LANES = 1>
 void add_plm_set(std::vector<StageLauncher>& v) {
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1, UNR, OCC, LANES>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MINMOD, UNR, OCC, LANES>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_MONOTIZED_CENTRAL, UNR, OCC, LANES>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS, UNR, OCC, LANES>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_SUPERBEE, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, HC_RECON_PLM_CONS, false, -1, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, HC_RECON_PLM_CONS, false, HC_LIMITER_MINMOD, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, HC_RECON_PLM_CONS, false, HC_LIMITER_MONOTIZED_CENTRAL, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, HC_RECON_PLM_CONS, false, HC_LIMITER_VAN_LEER_ABS, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, HC_RECON_PLM_CONS, false, HC_LIMITER_SUPERBEE, UNR, OCC, LANES>(v);
 }
 
 // Extra schedules for one compiled-in limiter (the batched configuration's)
 // and the generic kernel.
 template <typename T, int PREC, int DIM, int VAR, int TX, int TY, int TZ, int L, int NT, int UNR, int OCC = 0, int LANES = 1>
 void add_plm_pair(std::vector<StageLauncher>& v) {
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, -1, UNR, OCC, LANES>(v);
-    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, true, false, HC_LIMITER_VAN_LEER_ABS, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, HC_RECON_PLM_CONS, false, -1, UNR, OCC, LANES>(v);
+    add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, HC_RECON_PLM_CONS, false, HC_LIMITER_VAN_LEER_ABS, UNR, OCC, LANES>(v);
 }
 
 template <typename T, int PREC, int DIM, bool EXACT>

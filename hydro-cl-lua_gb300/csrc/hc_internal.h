@@ -88,6 +88,8 @@ struct PlainParams {
     int bc[6];
     int fluxLimiter, recon, slopeLimiter;
     double gamma, rhoMin, PMin;
+    int flux;             // HC_FLUX_*
+    int hllcMethod;       // euler-hllc's hllcMethod, 0..2
 };
 
 struct PlainSolver;   // defined in hc_plain.cu
@@ -112,6 +114,8 @@ struct FusedSet;      // defined in hc_fused.cu
 struct FusedScheme {
     int precision;     // HC_F32_FUSED or HC_F64_FUSED
     int flux_limiter, recon, slope_limiter, integrator;
+    int flux;          // HC_FLUX_*
+    int hllc_method;   // HC_HLLC_*
 };
 int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, FusedSet** out);
 void fused_destroy(FusedSet* f);
@@ -151,6 +155,7 @@ int fused_variant(const FusedSet* f, int dim);
 int fused_conservation(FusedSet* f, int slot, double sums[5]);
 int fused_stats(FusedSet* f, hc_batch_stats* st);
 int fused_autotune(FusedSet* f, const char* cache_path);
+int fused_set_schedule(FusedSet* f, int dim, int variant);
 int fused_sync(FusedSet* f);
 
 }  // namespace hc

@@ -31,6 +31,8 @@ struct B2 { bool x, y; };
 __device__ __forceinline__ bool any(bool m) { return m; }
 __device__ __forceinline__ bool any(B2 m) { return m.x || m.y; }
 __device__ __forceinline__ B2 operator||(B2 a, B2 b) { return {a.x || b.x, a.y || b.y}; }
+__device__ __forceinline__ bool lanesAnd(bool a, bool b) { return a && b; }
+__device__ __forceinline__ B2 lanesAnd(B2 a, B2 b) { return {a.x && b.x, a.y && b.y}; }
 
 template <typename V> struct MaskOf;
 template <> struct MaskOf<float> { using type = bool; };
@@ -56,6 +58,12 @@ __device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b,
 __device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 fnms(float2 a, float2 b, float2 c) { return __ffma2_rn(make_float2(-a.x, -a.y), b, c); }
+
+// -x (exact).  Scalar FMAs take a negated operand for free; a register pair
+// needs one packed multiply, so the formulas below negate shared operands once
+// and use fma(-a, b, c) where c - a b is meant.
+__device__ __forceinline__ float neg(float x) { return -x; }
+__device__ __forceinline__ float2 neg(float2 x) { return __fmul2_rn(x, make_float2(-1.f, -1.f)); }
 
 // ---- per-lane operations ----------------------------------------------------
 
@@ -91,6 +99,9 @@ template <typename V> constexpr int nlanes() { return sizeof(V) / sizeof(float);
 
 struct Eos {
     float gamma, g1, rhoMin, PMin;
+    int hllcMethod;   // euler-hllc's hllcMethod, 0..2
+    float invg1;      // 1 / (gamma - 1)
+    int recon;        // HC_RECON_*
 };
 
 // A conserved state in the interface frame: rho, m_n, m_t1, m_t2, ETotal.
@@ -99,7 +110,8 @@ template <typename V> struct C5 { V u[5]; };
 template <typename V> struct Eig {
     V vn, vt1, vt2, hT, Cs;
     V hvSq;          // |v|^2 / 2
-    V invD, invD2;   // 1 / (2 Cs^2), 2 / (2 Cs^2)
+    V invD;          // 1 / (2 Cs^2)
+    V nCs, nInvD2;   // -Cs, -2 / (2 Cs^2)
     Mask<V> ident;   // rho < rhoMin: the transforms are the identity
 };
 
@@ -108,14 +120,15 @@ template <typename V> struct Eig {
 // sqrt(rho) = rho rs, 1/rho = rs^2 and the Roe weights.
 template <typename V>
 __device__ __forceinline__ V eigenRoe(Eig<V>& e, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
-    V const half = splat<V>(.5f), g1 = splat<V>(s.g1), rhoMin = splat<V>(s.rhoMin), zero = splat<V>(0.f);
+    V const half = splat<V>(.5f), nhalf = splat<V>(-.5f), g1 = splat<V>(s.g1), rhoMin = splat<V>(s.rhoMin),
+            zero = splat<V>(0.f);
     V const rsL = rsq(UL.u[0]), rsR = rsq(UR.u[0]);
     V const invL = mul(rsL, rsL), invR = mul(rsR, rsR);
     V const sL = mul(UL.u[0], rsL), sR = mul(UR.u[0], rsR);
     V const m2L = fma(UL.u[3], UL.u[3], fma(UL.u[2], UL.u[2], mul(UL.u[1], UL.u[1])));
     V const m2R = fma(UR.u[3], UR.u[3], fma(UR.u[2], UR.u[2], mul(UR.u[1], UR.u[1])));
-    V const PL = sel(lt(UL.u[0], rhoMin), zero, mul(g1, fnms(mul(half, m2L), invL, UL.u[4])));
-    V const PR = sel(lt(UR.u[0], rhoMin), zero, mul(g1, fnms(mul(half, m2R), invR, UR.u[4])));
+    V const PL = sel(lt(UL.u[0], rhoMin), zero, mul(g1, fma(mul(nhalf, m2L), invL, UL.u[4])));
+    V const PR = sel(lt(UR.u[0], rhoMin), zero, mul(g1, fma(mul(nhalf, m2R), invR, UR.u[4])));
     V const invDen = rcp(add(sL, sR));
     e.vn = mul(fma(UL.u[1], rsL, mul(UR.u[1], rsR)), invDen);
     e.vt1 = mul(fma(UL.u[2], rsL, mul(UR.u[2], rsR)), invDen);
@@ -155,7 +168,8 @@ template <typename V>
 __device__ __forceinline__ void finishEig(Eig<V>& e, const Eos& s, V rho) {
     e.ident = lt(rho, splat<V>(s.rhoMin));
     e.invD = rcp(mul(mul(splat<V>(2.f), e.Cs), e.Cs));
-    e.invD2 = mul(splat<V>(2.f), e.invD);
+    e.nInvD2 = mul(splat<V>(-2.f), e.invD);
+    e.nCs = neg(e.Cs);
 }
 
 __device__ __forceinline__ void eigen(Eig<float>& e, const Eos& s, const C5<float>& UL, const C5<float>& UR) {
@@ -164,14 +178,10 @@ __device__ __forceinline__ void eigen(Eig<float>& e, const Eos& s, const C5<floa
     finishEig(e, s, rho);
 }
 
-__device__ __forceinline__ void eigen(Eig<float2>& e, const Eos& s, const C5<float2>& UL, const C5<float2>& UR) {
-    B2 const lv = lt(UL.u[0], splat<float2>(1e-5f)), rv = lt(UR.u[0], splat<float2>(1e-5f));
-    if (!any(lv || rv)) {
-        float2 const rho = eigenRoe(e, s, UL, UR);
-        finishEig(e, s, rho);
-        return;
-    }
-    // a vacuum side in either lane: each lane on its own
+// A lane pair with a vacuum side in either lane: each lane on its own.  Kept
+// out of line: it is rare, and inlined at every interface it would crowd the
+// instruction cache.
+static __device__ __noinline__ void eigenLanewise(Eig<float2>& e, const Eos& s, const C5<float2>& UL, const C5<float2>& UR) {
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         C5<float> l, r;
@@ -186,8 +196,19 @@ __device__ __forceinline__ void eigen(Eig<float2>& e, const Eos& s, const C5<flo
         setLane(e.Cs, k, e1.Cs);
         setLane(e.hvSq, k, e1.hvSq);
         setLane(e.invD, k, e1.invD);
-        setLane(e.invD2, k, e1.invD2);
+        setLane(e.nInvD2, k, e1.nInvD2);
+        setLane(e.nCs, k, e1.nCs);
         if (k) e.ident.y = e1.ident; else e.ident.x = e1.ident;
+    }
+}
+
+__device__ __forceinline__ void eigen(Eig<float2>& e, const Eos& s, const C5<float2>& UL, const C5<float2>& UR) {
+    B2 const lv = lt(UL.u[0], splat<float2>(1e-5f)), rv = lt(UR.u[0], splat<float2>(1e-5f));
+    if (!any(lv || rv)) {
+        float2 const rho = eigenRoe(e, s, UL, UR);
+        finishEig(e, s, rho);
+    } else {
+        eigenLanewise(e, s, UL, UR);
     }
 }
 
@@ -208,11 +229,12 @@ template <typename V>
 __device__ __forceinline__ void left(V* w, const Eig<V>& e, const Eos& s, const V* X) {
     V const mv = fma(X[3], e.vt2, fma(X[2], e.vt1, mul(X[1], e.vn)));
     V const q = mul(splat<V>(s.g1), fma(X[0], e.hvSq, sub(X[4], mv)));
-    V const kp = fnms(X[0], e.vn, X[1]);
-    w[0] = mul(fnms(e.Cs, kp, q), e.invD);
-    w[1] = fnms(q, e.invD2, X[0]);
-    w[2] = fnms(X[0], e.vt1, X[2]);
-    w[3] = fnms(X[0], e.vt2, X[3]);
+    V const nX0 = neg(X[0]);
+    V const kp = fma(nX0, e.vn, X[1]);
+    w[0] = mul(fma(e.nCs, kp, q), e.invD);
+    w[1] = fma(q, e.nInvD2, X[0]);
+    w[2] = fma(nX0, e.vt1, X[2]);
+    w[3] = fma(nX0, e.vt2, X[3]);
     w[4] = mul(fma(e.Cs, kp, q), e.invD);
     identLanes(w, e, X);
 }
@@ -241,27 +263,173 @@ __device__ __forceinline__ void right(V* F, const Eig<V>& e, const V* W) {
     identLanes(F, e, W);
 }
 
-// Roe flux without a flux limiter (roe.cl:17-163) from the one-sided
-// projections: lambda L.(UL+UR)/2 - |lambda| L.(UR-UL)/2 equals
-// max(lambda, 0) L.UL + min(lambda, 0) L.UR component by component.
+// fluxFromCons (euler.cl:271-291) in the interface frame:
+// (rho v_n, m_n v_n + P, m_t1 v_n, m_t2 v_n, (ETotal + P) v_n); also v_n and P.
 template <typename V>
-__device__ __forceinline__ void roeSplit(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+__device__ __forceinline__ void fluxOf(V* F, V& P, const Eos& s, const C5<V>& U) {
+    V const inv = rcp(U.u[0]);
+    V const vn = mul(U.u[1], inv);
+    V const m2 = fma(U.u[3], U.u[3], fma(U.u[2], U.u[2], mul(U.u[1], U.u[1])));
+    P = sel(lt(U.u[0], splat<V>(s.rhoMin)), splat<V>(0.f),
+            mul(splat<V>(s.g1), fma(mul(splat<V>(-.5f), m2), inv, U.u[4])));
+    F[0] = mul(U.u[0], vn);
+    F[1] = fma(U.u[1], vn, P);
+    F[2] = mul(U.u[2], vn);
+    F[3] = mul(U.u[3], vn);
+    F[4] = mul(add(U.u[4], P), vn);
+}
+
+// The slowest and fastest waves v_n -/+ Cs of one state (euler.lua:329-337):
+// Cs = 0 where P <= PMin, infinite where rho < rhoMin; v_n = 0 where rho < rhoMin.
+template <typename V>
+__device__ __forceinline__ void wavesOf(V& lmin, V& lmax, const Eos& s, const C5<V>& U, V P) {
+    V const inv = rcp(U.u[0]);
+    auto const thin = lt(U.u[0], splat<V>(s.rhoMin));
+    V Cs = sqr(mul(mul(splat<V>(s.gamma), P), inv));
+    Cs = sel(thin, splat<V>(__int_as_float(0x7f800000)), Cs);
+    Cs = sel(le(P, splat<V>(s.PMin)), splat<V>(0.f), Cs);
+    V const vn = sel(thin, splat<V>(0.f), mul(U.u[1], inv));
+    lmin = sub(vn, Cs);
+    lmax = add(vn, Cs);
+}
+
+// Rusanov flux (hydro/flux/rusanov.cl): .5 (FL + FR - lambda (UR - UL)) with
+// lambda = max(|v_n - Cs|, |v_n + Cs|) of the right state (the reference's
+// loop over the two sides keeps the last one's bound).
+template <typename V>
+__device__ __forceinline__ void rusanov(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+    V FL[5], FR[5], PL, PR, lmin, lmax;
+    fluxOf(FL, PL, s, UL);
+    fluxOf(FR, PR, s, UR);
+    wavesOf(lmin, lmax, s, UR, PR);
+    V const nlam = neg(vmax(absv(lmin), absv(lmax)));
+    V const half = splat<V>(.5f);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) F[j] = mul(half, fma(nlam, sub(UR.u[j], UL.u[j]), add(FL[j], FR[j])));
+}
+
+// HLL flux (hydro/flux/hll.cl, waves 'Davis direct bounded'): sL = min(v_n - Cs
+// of UL, Roe-average v_n - Cs), sR = max(v_n + Cs of UR, Roe-average v_n + Cs);
+// FL where 0 <= sL, FR where sR <= 0, else
+// (sR FL - sL FR + sL sR (UR - UL)) / (sR - sL).
+template <typename V>
+__device__ __forceinline__ void hll(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
     Eig<V> e;
     eigen(e, s, UL, UR);
-    V wL[5], wR[5], fe[5];
-    left(wL, e, s, UL.u);
-    left(wR, e, s, UR.u);
+    V FL[5], FR[5], PL, PR, lminL, lmaxL, lminR, lmaxR;
+    fluxOf(FL, PL, s, UL);
+    fluxOf(FR, PR, s, UR);
+    wavesOf(lminL, lmaxL, s, UL, PL);
+    wavesOf(lminR, lmaxR, s, UR, PR);
+    V const sL = vmin(lminL, sub(e.vn, e.Cs));
+    V const sR = vmax(lmaxR, add(e.vn, e.Cs));
+    V const inv = rcp(sub(sR, sL));
+    V const sLsR = mul(sL, sR);
+    V const nsL = neg(sL);
     V const zero = splat<V>(0.f);
-    V const l0 = sub(e.vn, e.Cs), l4 = add(e.vn, e.Cs);
-    V const p0 = vmax(l0, zero), m0 = vmin(l0, zero);
-    V const p1 = vmax(e.vn, zero), m1 = vmin(e.vn, zero);
-    V const p4 = vmax(l4, zero), m4 = vmin(l4, zero);
-    fe[0] = fma(p0, wL[0], mul(m0, wR[0]));
-    fe[1] = fma(p1, wL[1], mul(m1, wR[1]));
-    fe[2] = fma(p1, wL[2], mul(m1, wR[2]));
-    fe[3] = fma(p1, wL[3], mul(m1, wR[3]));
-    fe[4] = fma(p4, wL[4], mul(m4, wR[4]));
+    auto const left = le(zero, sL), right = le(sR, zero);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        V const mid = mul(fma(sLsR, sub(UR.u[j], UL.u[j]), fma(nsL, FR[j], mul(sR, FL[j]))), inv);
+        F[j] = sel(left, FL[j], sel(right, FR[j], mid));
+    }
+}
+
+// Roe flux without a flux limiter (roe.cl:17-163) in the fluxFromCons form
+// Euler inherits (roeUseFluxFromCons, eqn.lua:46):
+//   F = (F(UL) + F(UR)) / 2 - R |Lambda| L.(UR - UL) / 2.
+template <typename V>
+__device__ __forceinline__ void roe(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+    Eig<V> e;
+    eigen(e, s, UL, UR);
+    V dU[5], dW[5], fe[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) dU[j] = sub(UR.u[j], UL.u[j]);
+    left(dW, e, s, dU);
+    V const nh = splat<V>(-.5f);
+    V const c0 = mul(nh, absv(sub(e.vn, e.Cs)));
+    V const c1 = mul(nh, absv(e.vn));
+    V const c4 = mul(nh, absv(add(e.vn, e.Cs)));
+    fe[0] = mul(c0, dW[0]);
+    fe[1] = mul(c1, dW[1]);
+    fe[2] = mul(c1, dW[2]);
+    fe[3] = mul(c1, dW[3]);
+    fe[4] = mul(c4, dW[4]);
     right(F, e, fe);
+    V FL[5], FR[5], PL, PR;
+    fluxOf(FL, PL, s, UL);
+    fluxOf(FR, PR, s, UR);
+    V const half = splat<V>(.5f);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) F[j] = fma(half, add(FL[j], FR[j]), F[j]);
+}
+
+// HLLC flux (hydro/flux/euler-hllc.cl, 2012 Toro; waves as hll) in the
+// interface frame.  The star state of side K (speed sK):
+//   method 0: F = FK + sK (UK* - UK), rho* = rho (sK - vn) / (sK - s*),
+//             m* = rho* (s*, vt1, vt2), E* = rho* (E / rho + (s* - vn)(s* + P / (rho (sK - vn))))
+//   method 1: F = (s* (sK U - FK) + sK (P + rho (sK - vn)(s* - vn)) (0, 1, 0, 0, s*)) / (sK - s*)
+//   method 2: as method 1 with P + rho (sK - vn)(s* - vn) replaced by the
+//             average PLR of the two sides
+// chosen, lane by lane, in the reference's order: FL where 0 <= sL, the left
+// star where sL <= 0 <= s*, the right star where s* <= 0 <= sR, FR where
+// sR <= 0, else the HLL average.
+template <typename V>
+__device__ __forceinline__ void hllc(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+    Eig<V> e;
+    eigen(e, s, UL, UR);
+    V FL[5], FR[5], PL, PR, lminL, lmaxL, lminR, lmaxR;
+    fluxOf(FL, PL, s, UL);
+    fluxOf(FR, PR, s, UR);
+    wavesOf(lminL, lmaxL, s, UL, PL);
+    wavesOf(lminR, lmaxR, s, UR, PR);
+    V const sL = vmin(lminL, sub(e.vn, e.Cs));
+    V const sR = vmax(lmaxR, add(e.vn, e.Cs));
+    V const vnL = mul(UL.u[1], rcp(UL.u[0])), vnR = mul(UR.u[1], rcp(UR.u[0]));
+    V const aL = sub(sL, vnL), aR = sub(sR, vnR);   // sK - vn
+    V const rhoaL = mul(UL.u[0], aL), rhoaR = mul(UR.u[0], aR);
+    // s* = (rhoR vnR aR - rhoL vnL aL + PL - PR) / (rhoR aR - rhoL aL)
+    V const sStar = mul(sub(add(fma(rhoaR, vnR, neg(mul(rhoaL, vnL))), PL), PR), rcp(sub(rhoaR, rhoaL)));
+    V SL[5], SR[5];
+    auto star = [&](V* S, const C5<V>& U, const V* FK, V P, V sK, V a, V rhoa) {
+        V const d = rcp(sub(sK, sStar));
+        if (s.hllcMethod == 0) {
+            V const rs = mul(mul(U.u[0], a), d);
+            V const us[5] = {rs, mul(rs, sStar), mul(rs, mul(U.u[2], rcp(U.u[0]))), mul(rs, mul(U.u[3], rcp(U.u[0]))),
+                             mul(rs, fma(sub(sStar, sub(sK, a)), add(sStar, mul(P, rcp(rhoa))), mul(U.u[4], rcp(U.u[0]))))};
+#pragma unroll
+            for (int j = 0; j < 5; ++j) S[j] = fma(sK, sub(us[j], U.u[j]), FK[j]);
+        } else {
+            V const vn = sub(sK, a);
+            V const Pk = s.hllcMethod == 1
+                ? fma(rhoa, sub(sStar, vn), P)
+                : mul(splat<V>(.5f), add(add(add(PL, PR), mul(rhoaL, sub(sStar, vnL))), mul(rhoaR, sub(sStar, vnR))));
+#pragma unroll
+            for (int j = 0; j < 5; ++j) S[j] = mul(sStar, sub(mul(sK, U.u[j]), FK[j]));
+            S[1] = fma(sK, Pk, S[1]);
+            S[4] = fma(mul(sK, Pk), sStar, S[4]);
+#pragma unroll
+            for (int j = 0; j < 5; ++j) S[j] = mul(S[j], d);
+        }
+    };
+    star(SL, UL, FL, PL, sL, aL, rhoaL);
+    star(SR, UR, FR, PR, sR, aR, rhoaR);
+    V const zero = splat<V>(0.f);
+    V const inv = rcp(sub(sR, sL));
+    V const sLsR = mul(sL, sR);
+    V const nsL = neg(sL);
+    auto const c0 = le(zero, sL), c3 = le(sR, zero);
+    auto const c1 = le(sL, zero);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        V const avg = mul(fma(sLsR, sub(UR.u[j], UL.u[j]), fma(nsL, FR[j], mul(sR, FL[j]))), inv);
+        V r = avg;
+        r = sel(c3, FR[j], r);
+        r = sel(lanesAnd(le(sStar, zero), le(zero, sR)), SR[j], r);
+        r = sel(lanesAnd(c1, le(zero, sStar)), SL[j], r);
+        r = sel(c0, FL[j], r);
+        F[j] = r;
+    }
 }
 
 // Half slope .5 phi(r) dU of "plm cons" (plm.cl:27-91) for a limiter fixed at
@@ -317,6 +485,119 @@ __device__ __forceinline__ float2 halfSlope(float2 dUL, float2 dUR, int limRT) {
     }
 }
 
+// ---- "plm prim" and "plm athena" ---------------------------------------------
+
+// primFromCons (euler.cl:140-159) in the interface frame: rho, v_n, v_t1, v_t2, P.
+template <typename V>
+__device__ __forceinline__ void primOf(V* w, const Eos& s, const C5<V>& U) {
+    V const inv = rcp(U.u[0]);
+    V const m2 = fma(U.u[3], U.u[3], fma(U.u[2], U.u[2], mul(U.u[1], U.u[1])));
+    w[0] = U.u[0];
+    w[1] = mul(U.u[1], inv);
+    w[2] = mul(U.u[2], inv);
+    w[3] = mul(U.u[3], inv);
+    w[4] = sel(lt(U.u[0], splat<V>(s.rhoMin)), splat<V>(0.f),
+               mul(splat<V>(s.g1), fma(mul(splat<V>(-.5f), m2), inv, U.u[4])));
+}
+
+// consFromPrim (euler.cl:163-173) in the interface frame.
+template <typename V>
+__device__ __forceinline__ void consOf(C5<V>& U, const Eos& s, const V* w) {
+    U.u[0] = w[0];
+    U.u[1] = mul(w[1], w[0]);
+    U.u[2] = mul(w[2], w[0]);
+    U.u[3] = mul(w[3], w[0]);
+    V const vsq = fma(w[3], w[3], fma(w[2], w[2], mul(w[1], w[1])));
+    U.u[4] = fma(w[4], splat<V>(s.invg1), mul(w[0], mul(splat<V>(.5f), vsq)));
+}
+
+// "plm prim"'s half slope .5 phi(r) dWR with r = dWL / dWR (0 where dWR = 0),
+// from the reference's limiter table (plm.cl:223-231).
+__device__ __forceinline__ float halfSlopePrim(float dWL, float dWR, int lim) {
+    float const r = dWR == 0.f ? 0.f : __fdiv_rn(dWL, dWR);
+    return mul(.5f, mul(fast::limiter<float>(lim, r), dWR));
+}
+__device__ __forceinline__ float2 halfSlopePrim(float2 dWL, float2 dWR, int lim) {
+    return make_float2(halfSlopePrim(dWL.x, dWR.x, lim), halfSlopePrim(dWL.y, dWR.y, lim));
+}
+
+// "plm prim" (plm.cl:191-253): the cell's L and R states from its own and
+// its neighbours' primitives.
+template <typename V>
+__device__ __forceinline__ void plmPrim(C5<V>& L, C5<V>& R, const Eos& s, const V* Wm, const V* W0, const V* Wp,
+                                        int lim) {
+    V nL[5], nR[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        V const h = halfSlopePrim(sub(W0[j], Wm[j]), sub(Wp[j], W0[j]), lim);
+        nL[j] = sub(W0[j], h);
+        nR[j] = add(W0[j], h);
+    }
+    consOf(L, s, nL);
+    consOf(R, s, nR);
+}
+
+// "plm athena" (plm.cl:782-879): the primitive differences projected on the
+// eigenvectors at the cell (eigen_forCell, euler.cl:315-342), limited per
+// wave (zero unless the left and right projections agree in sign, else
+// sign(c) min(2 min(|l|, |r|), min(|c|, |g|)) with the central and the
+// harmonic differences c and g), projected back, clamped into the range of
+// the neighbouring primitives; L is built from the right-edge value and R
+// from the left-edge value, as plm.cl:877-878 assigns them.
+template <typename V>
+__device__ __forceinline__ void plmAthena(C5<V>& L, C5<V>& R, const Eos& s, const C5<V>& U0, const V* Wm,
+                                          const V* W0, const V* Wp) {
+    V const zero = splat<V>(0.f), half = splat<V>(.5f), two = splat<V>(2.f);
+    Eig<V> e;
+    e.vn = W0[1];
+    e.vt1 = W0[2];
+    e.vt2 = W0[3];
+    e.hvSq = mul(half, fma(W0[3], W0[3], fma(W0[2], W0[2], mul(W0[1], W0[1]))));
+    e.hT = mul(add(W0[4], U0.u[4]), rcp(W0[0]));
+    e.Cs = sqr(mul(splat<V>(s.g1), sub(e.hT, e.hvSq)));
+    finishEig(e, s, W0[0]);
+    V dWL[5], dWR[5], dWC[5], dWG[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        dWL[j] = sub(W0[j], Wm[j]);
+        dWR[j] = sub(Wp[j], W0[j]);
+        dWC[j] = mul(half, sub(Wp[j], Wm[j]));
+        V const g = mul(mul(mul(two, dWL[j]), dWR[j]), rcp(add(dWL[j], dWR[j])));
+        dWG[j] = sel(le(mul(dWL[j], dWR[j]), zero), zero, g);
+    }
+    V dal[5], dar[5], dac[5], dag[5];
+    left(dal, e, s, dWL);
+    left(dar, e, s, dWR);
+    left(dac, e, s, dWC);
+    left(dag, e, s, dWG);
+    V da[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        V const m = vmin(mul(two, vmin(absv(dal[j]), absv(dar[j]))), vmin(absv(dac[j]), absv(dag[j])));
+        V const sm = sel(gt(dac[j], zero), m, sel(lt(dac[j], zero), neg(m), zero));
+        da[j] = sel(gt(mul(dal[j], dar[j]), zero), sm, zero);
+    }
+    V dWm[5];
+    right(dWm, e, da);
+    V lv[5], rv[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        V l = fnms(half, dWm[j], W0[j]);
+        V r = fma(half, dWm[j], W0[j]);
+        V const C = add(r, l);
+        l = vmax(vmin(W0[j], Wm[j]), l);
+        l = vmin(vmax(W0[j], Wm[j]), l);
+        r = sub(C, l);
+        r = vmax(vmin(W0[j], Wp[j]), r);
+        r = vmin(vmax(W0[j], Wp[j]), r);
+        l = sub(C, r);
+        lv[j] = l;
+        rv[j] = r;
+    }
+    consOf(L, s, rv);
+    consOf(R, s, lv);
+}
+
 }  // namespace lanes
 }  // namespace hc
 
@@ -326,22 +607,29 @@ namespace lanes {
 // ---- the per-cell epilogue ----------------------------------------------------
 
 // constrainU (euler.cl:697-717): rho >= rhoMin, P >= PMin, through the
-// primitive variables and back.
+// primitive variables and back.  A cell that needs neither clamp keeps its
+// state: the round trip is the identity in exact arithmetic, and in FP32 it
+// is not (P (1/(g-1)) with both factors rounded adds 1.5e-8 of the internal
+// energy per stage at g = 1.4, a drift of the total energy).
 template <typename V>
 __device__ __forceinline__ void constrain(V* u, const Eos& s, float invg1) {
     V const rhoMin = splat<V>(s.rhoMin);
-    u[0] = vmax(u[0], rhoMin);
-    V const inv = rcp(u[0]);
-    V const vx = mul(u[1], inv), vy = mul(u[2], inv), vz = mul(u[3], inv);
+    auto const thin = lt(u[0], rhoMin);
+    V const rho = vmax(u[0], rhoMin);
+    V const inv = rcp(rho);
     V const m2 = fma(u[3], u[3], fma(u[2], u[2], mul(u[1], u[1])));
-    V P = sel(lt(u[0], rhoMin), splat<V>(0.f), mul(splat<V>(s.g1), fnms(mul(splat<V>(.5f), m2), inv, u[4])));
-    P = vmax(P, splat<V>(s.PMin));
-    V const rho = u[0];
-    u[1] = mul(vx, rho);
-    u[2] = mul(vy, rho);
-    u[3] = mul(vz, rho);
+    V const P0 = mul(splat<V>(s.g1), fma(mul(splat<V>(-.5f), m2), inv, u[4]));
+    auto const low = lt(P0, splat<V>(s.PMin));
+    if (!any(thin || low)) return;
+    V const vx = mul(u[1], inv), vy = mul(u[2], inv), vz = mul(u[3], inv);
+    V const P = vmax(P0, splat<V>(s.PMin));
     V const vsq = fma(vz, vz, fma(vy, vy, mul(vx, vx)));
-    u[4] = fma(P, splat<V>(invg1), mul(rho, mul(splat<V>(.5f), vsq)));
+    auto const fix = thin || low;
+    u[0] = rho;
+    u[1] = sel(fix, mul(vx, rho), u[1]);
+    u[2] = sel(fix, mul(vy, rho), u[2]);
+    u[3] = sel(fix, mul(vz, rho), u[3]);
+    u[4] = sel(fix, fma(P, splat<V>(invg1), mul(rho, mul(splat<V>(.5f), vsq))), u[4]);
 }
 
 // calcDTCell (calcDT.cl:38-73): min over the active sides of
@@ -353,7 +641,7 @@ __device__ __forceinline__ V dtCell(const V* u, const Eos& s, const float* gdx) 
     auto const thin = lt(u[0], rhoMin);
     V const inv = rcp(u[0]);
     V const m2 = fma(u[3], u[3], fma(u[2], u[2], mul(u[1], u[1])));
-    V const P = sel(thin, zero, mul(splat<V>(s.g1), fnms(mul(splat<V>(.5f), m2), inv, u[4])));
+    V const P = sel(thin, zero, mul(splat<V>(s.g1), fma(mul(splat<V>(-.5f), m2), inv, u[4])));
     V Cs = sqr(mul(mul(splat<V>(s.gamma), P), inv));
     Cs = sel(thin, splat<V>(__int_as_float(0x7f800000)), Cs);
     Cs = sel(le(P, splat<V>(s.PMin)), zero, Cs);

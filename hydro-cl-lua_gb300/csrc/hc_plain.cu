@@ -40,6 +40,9 @@ __device__ __forceinline__ Eos eosOf(const PlainParams& s) {
     Eos e;
     e.gamma = s.gamma; e.rhoMin = s.rhoMin; e.PMin = s.PMin;
     e.fluxLimiter = s.fluxLimiter; e.slopeLimiter = s.slopeLimiter;
+    e.flux = s.flux;
+    e.hllcMethod = s.hllcMethod;
+    e.recon = s.recon;
     return e;
 }
 
@@ -117,10 +120,10 @@ __global__ void k_calcLR(PlainParams s, const Cons* Ub, Cons* ULR) {
     Cons const U = Ub[index];
     for (int side = 0; side < s.dim; ++side) {
         Cons L = U, R = U;
-        if (s.recon == HC_RECON_PLM_CONS) {
+        if (s.recon >= HC_RECON_PLM_CONS) {
             Cons const UL = Ub[index - s.stepsize[side]];
             Cons const UR = Ub[index + s.stepsize[side]];
-            ref::plmCons(L.p, R.p, e, UL.p, U.p, UR.p);
+            ref::plmAny(L.p, R.p, e, UL.p, U.p, UR.p, side);
         }
         ULR[2 * (side + s.dim * index) + 0] = L;
         ULR[2 * (side + s.dim * index) + 1] = R;
@@ -134,7 +137,8 @@ __global__ void k_calcFlux(PlainParams s, const Cons* Ub, const Cons* ULR, Cons*
     cellCoords(s, index, i);
     if (oob(s, i, kGhost, kGhost - 1)) return;
     bool const usePLM = s.recon != HC_RECON_NONE;
-    bool const lim = s.fluxLimiter > 0;
+    // only the Roe flux takes the flux limiter (fvsolver.lua:62-64)
+    bool const lim = s.fluxLimiter > 0 && s.flux == HC_FLUX_ROE;
     for (int side = 0; side < s.dim; ++side) {
         double const dx = s.grid_dx[side];
         long long const indexR = index;
@@ -164,6 +168,24 @@ __global__ void k_calcFlux(PlainParams s, const Cons* Ub, const Cons* ULR, Cons*
             lr(indexR, indexR + s.stepsize[side], UL_R, UR_R);
         }
         Eos const e = eosOf(s);
+        if (s.flux == HC_FLUX_RUSANOV) {
+            double out[6];
+            ref::rusanovFlux(out, e, UL, UR, side);
+            for (int j = 0; j < 5; ++j) F.p[j] = out[j];
+            continue;
+        }
+        if (s.flux == HC_FLUX_HLL || s.flux == HC_FLUX_HLLC) {
+            // a NaN wave bound assigns nothing: the flux buffer keeps its
+            // previous content, as in the reference
+            ref::Eig eig;
+            ref::eigenForInterface(eig, e, UL, UR);
+            double out[6];
+            bool const set = s.flux == HC_FLUX_HLL ? ref::hllFlux(out, e, UL, UR, side, eig)
+                                                   : ref::hllcFlux(out, e, UL, UR, side, eig);
+            if (set)
+                for (int j = 0; j < 6; ++j) F.p[j] = out[j];
+            continue;
+        }
         ref::Iface C, IL, IR;
         ref::makeIface(C, e, UL, UR, side);
         if (lim) {
@@ -336,6 +358,8 @@ int plain_create(const hc_solver_desc& d, cudaStream_t stream, PlainSolver** out
     p.fluxLimiter = d.flux_limiter;
     p.recon = d.recon;
     p.slopeLimiter = d.slope_limiter;
+    p.flux = d.flux;
+    p.hllcMethod = d.hllc_method == HC_HLLC_DEFAULT ? 2 : d.hllc_method - 1;
     p.gamma = d.gamma;
     p.rhoMin = d.rho_min;
     p.PMin = d.p_min;

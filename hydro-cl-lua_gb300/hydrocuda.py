@@ -42,7 +42,9 @@ INTEGRATORS = [
     "Runge-Kutta 2, non-TVD", "Runge-Kutta 3, TVD", "Runge-Kutta 4, TVD", "Runge-Kutta 4, non-TVD",
 ]
 BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3}
-RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2}
+RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2, "plm prim": 3, "plm athena": 4}
+# hydro/flux/*.lua names
+FLUXES = ["roe", "hll", "rusanov", "euler-hllc"]
 PRECISIONS = {"f64 plain": 0, "f64": 1, "f32": 2}
 LAYOUTS = {"aos6": 0, "soa5": 1, "soa5_f32": 2}
 SIDES = ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")
@@ -67,6 +69,7 @@ class SolverDesc(ctypes.Structure):
         ("integrator", ctypes.c_int), ("precision", ctypes.c_int),
         ("gamma", ctypes.c_double), ("rho_min", ctypes.c_double), ("p_min", ctypes.c_double),
         ("cfl", ctypes.c_double), ("fixed_dt", ctypes.c_double),
+        ("flux", ctypes.c_int), ("hllc_method", ctypes.c_int),
     ]
 
 
@@ -74,7 +77,7 @@ class BatchDesc(ctypes.Structure):
     _fields_ = [
         ("precision", ctypes.c_int), ("flux_limiter", ctypes.c_int), ("recon", ctypes.c_int),
         ("slope_limiter", ctypes.c_int), ("integrator", ctypes.c_int), ("max_slots", ctypes.c_int),
-        ("hbm_budget", ctypes.c_size_t),
+        ("hbm_budget", ctypes.c_size_t), ("flux", ctypes.c_int), ("hllc_method", ctypes.c_int),
     ]
 
 
@@ -138,6 +141,7 @@ PROTOTYPES = {
     "hc_batch_stats_get": (_ip, [_vp, ctypes.POINTER(BatchStats)]),
     "hc_batch_conservation": (_ip, [_vp, _ip, _dp]),
     "hc_batch_autotune": (_ip, [_vp, ctypes.c_char_p]),
+    "hc_batch_set_schedule": (_ip, [_vp, _ip, _ip]),
     "hc_calc_dt_noalloc": (_ip, [ctypes.POINTER(SolverDesc), _vp, _vp, _vp]),
 }
 
@@ -250,8 +254,9 @@ def make_desc(args):
     dim = int(args["dim"])
     if args.get("eqn", "euler") != "euler":
         raise ValueError("only eqn='euler' is provided")
-    if args.get("flux", "roe") != "roe":
-        raise ValueError("only flux='roe' is provided")
+    d.flux = _index(FLUXES, args.get("flux", "roe"), "flux")
+    # euler-hllc's hllcMethod (0, 1, 2; the reference's default 2); 0 in the descriptor is that default
+    d.hllc_method = int(args["hllcMethod"]) + 1 if "hllcMethod" in args else 0
     if args.get("coord", "cartesian") != "cartesian":
         raise ValueError("only coord='cartesian' is provided")
     gs = args["gridSize"]
@@ -421,7 +426,7 @@ class Batch:
 
     def __init__(self, ctx=None, precision="f32", usePLM=None, slopeLimiter="donor cell",
                  fluxLimiter="donor cell", integrator="forward Euler", max_slots=1024,
-                 hbm_budget=150 * (1 << 30)):
+                 hbm_budget=150 * (1 << 30), flux="roe", hllcMethod=None):
         self.ctx = ctx or default_context()
         self.L = self.ctx.L
         d = BatchDesc()
@@ -432,9 +437,13 @@ class Batch:
         d.integrator = _index(INTEGRATORS, integrator, "integrator")
         d.max_slots = int(max_slots)
         d.hbm_budget = int(hbm_budget)
+        d.flux = _index(FLUXES, flux, "flux")
+        d.hllc_method = int(hllcMethod) + 1 if hllcMethod is not None else 0
         self.desc = d
         self.scheme = dict(precision=precision, usePLM=usePLM, slopeLimiter=slopeLimiter,
-                           fluxLimiter=fluxLimiter, integrator=integrator)
+                           fluxLimiter=fluxLimiter, integrator=integrator, flux=flux)
+        if hllcMethod is not None:
+            self.scheme["hllcMethod"] = hllcMethod
         self.h = ctypes.c_void_p()
         _check(self.L.hc_batch_create(self.ctx.h, ctypes.byref(d), ctypes.byref(self.h)))
         self.slot_desc = {}
@@ -543,6 +552,11 @@ class Batch:
         s = (ctypes.c_double * 5)()
         _check(self.L.hc_batch_conservation(self.h, int(slot), s))
         return np.array(list(s))
+
+    def set_schedule(self, dim, variant):
+        """Pins the stage kernel's schedule for grids of dimension `dim` (the
+        autotuner log's variant number)."""
+        _check(self.L.hc_batch_set_schedule(self.h, int(dim), int(variant)))
 
     def autotune(self, cache_path=None):
         _check(self.L.hc_batch_autotune(self.h, cache_path.encode() if cache_path else None))

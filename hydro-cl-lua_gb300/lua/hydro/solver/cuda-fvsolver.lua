@@ -1,7 +1,8 @@
 --[[
-A 'cuda' Roe finite-volume solver for hydro-cl-lua: same args table as
-hydro/solver/fvsolver.lua (eqn='euler', flux='roe', coord='cartesian'), with
-the update -- boundary, calcLR ("plm cons"), calcFlux (Roe), calcDerivFromFlux,
+A 'cuda' finite-volume solver for hydro-cl-lua: same args table as
+hydro/solver/fvsolver.lua (eqn='euler', flux='roe', 'hll' or 'rusanov',
+coord='cartesian'), with the update -- boundary, calcLR ("plm cons"), calcFlux,
+calcDerivFromFlux,
 the integrator's multAdd sequence, constrainU, calcDT -- run by libhydrocuda on
 one GPU instead of by the OpenCL kernels.
 
@@ -32,7 +33,7 @@ local sharedCtx
 
 local function descFromSolver(self, args)
 	assert(self.eqn.name == 'euler', "the cuda solver provides eqn='euler'")
-	assert(self.flux.name == 'roe', "the cuda solver provides flux='roe'")
+	local flux = assert(hc.fluxIndex[self.flux.name], "the cuda solver provides flux='roe', 'hll', 'rusanov' and 'euler-hllc'")
 	assert(require 'hydro.coord.cartesian':isa(self.coord), "the cuda solver provides coord='cartesian'")
 	local d = ffi.new'hc_solver_desc'
 	d.dim = self.dim
@@ -50,7 +51,7 @@ local function descFromSolver(self, args)
 		end
 	end
 	d.flux_limiter = self.fluxLimiter - 1
-	d.recon = self.usePLM and assert(hc.reconIndex[self.usePLM], "the cuda solver provides usePLM='plm cons' and 'piecewise constant'") or 0
+	d.recon = self.usePLM and assert(hc.reconIndex[self.usePLM], "the cuda solver provides usePLM='piecewise constant', 'plm cons', 'plm prim' and 'plm athena'") or 0
 	d.slope_limiter = self.slopeLimiter - 1
 	d.integrator = assert(hc.integratorIndex[self.integrator.name], "the cuda solver provides the explicit integrators")
 	d.precision = hc.precisionIndex[args.cudaPrecision or 'f64 plain']
@@ -60,6 +61,8 @@ local function descFromSolver(self, args)
 	d.p_min = solverPtr.PMin
 	d.cfl = self.cfl
 	d.fixed_dt = self.useFixedDT and self.fixedDT or 0
+	d.flux = flux
+	d.hllc_method = self.flux.hllcMethod and (self.flux.hllcMethod + 1) or 0
 	return d
 end
 

@@ -26,6 +26,8 @@ typedef struct hc_solver_desc {
 	double p_min;
 	double cfl;
 	double fixed_dt;
+	int flux;
+	int hllc_method;
 } hc_solver_desc;
 typedef struct hc_context hc_context;
 typedef struct hc_solver hc_solver;
@@ -71,7 +73,8 @@ for i, name in ipairs{
 } do M.integratorIndex[name] = i - 1 end
 
 M.boundaryIndex = {none = 0, periodic = 1, mirror = 2, freeflow = 3}
-M.reconIndex = {['piecewise constant'] = 1, ['plm cons'] = 2}
+M.fluxIndex = {roe = 0, hll = 1, rusanov = 2, ['euler-hllc'] = 3}
+M.reconIndex = {['piecewise constant'] = 1, ['plm cons'] = 2, ['plm prim'] = 3, ['plm athena'] = 4}
 M.precisionIndex = {['f64 plain'] = 0, f64 = 1, f32 = 2}
 M.LAYOUT_AOS6_F64 = 0
 

@@ -89,6 +89,24 @@ extern "C" {
 #define HC_RECON_NONE                0   /* usePLM = nil: interface states are the cell states */
 #define HC_RECON_PIECEWISE_CONSTANT  1   /* "piecewise constant" */
 #define HC_RECON_PLM_CONS            2   /* "plm cons" */
+#define HC_RECON_PLM_PRIM            3   /* "plm prim" (plm.cl:191-253) */
+#define HC_RECON_PLM_ATHENA          4   /* "plm athena" (plm.cl:782-879, with its L/R assignment) */
+#define HC_NUM_RECONS                5
+
+/* interface flux (hydro/flux/*.lua); the flux limiter applies to Roe only
+ * (fvsolver.lua:62-64) */
+#define HC_FLUX_ROE      0   /* "roe" (roe.cl) */
+#define HC_FLUX_HLL      1   /* "hll", waves 'Davis direct bounded' (hll.cl) */
+#define HC_FLUX_RUSANOV  2   /* "rusanov" (rusanov.cl) */
+#define HC_FLUX_HLLC     3   /* "euler-hllc" (euler-hllc.cl), waves as hll */
+#define HC_NUM_FLUXES    4
+
+/* euler-hllc's hllcMethod (2012 Toro): HC_HLLC_DEFAULT is the reference's
+ * default, its method 2 */
+#define HC_HLLC_DEFAULT  0
+#define HC_HLLC_METHOD_0 1   /* Toro eqns 38-39 */
+#define HC_HLLC_METHOD_1 2   /* variation 1 */
+#define HC_HLLC_METHOD_2 3   /* variation 2 */
 
 /* explicit integrators (hydro/int/all.lua) */
 #define HC_INT_FORWARD_EULER   0
@@ -135,6 +153,8 @@ typedef struct hc_solver_desc {
     double p_min;            /* reference default 1e-7 */
     double cfl;              /* reference default .5 */
     double fixed_dt;         /* > 0: useFixedDT with this dt; <= 0: CFL dt */
+    int    flux;             /* HC_FLUX_* (0 = roe) */
+    int    hllc_method;      /* HC_HLLC_* (euler-hllc only) */
 } hc_solver_desc;
 
 /* Initial conditions generated on the device (the reference builds every
@@ -234,6 +254,8 @@ typedef struct hc_batch_desc {
     int    integrator;
     int    max_slots;        /* slot table size */
     size_t hbm_budget;       /* bytes of device state the batch may hold */
+    int    flux;             /* HC_FLUX_* shared by every instance (0 = roe) */
+    int    hllc_method;      /* HC_HLLC_* (euler-hllc only) */
 } hc_batch_desc;
 
 typedef struct hc_done {
@@ -286,6 +308,10 @@ int hc_batch_conservation(hc_batch* b, int slot, double sums[5]);
 /* Times the candidate tile shapes on the batch's current work list and keeps
  * the fastest; reads/writes the choice from/to cache_path when not NULL. */
 int hc_batch_autotune(hc_batch* b, const char* cache_path);
+/* Pins the schedule (tile shape, segment length, threads, lanes: the
+ * `variant` numbers of the autotuner's log) of the stage kernel for grids of
+ * dimension `dim`.  HC_ERR_INVALID if this scheme has no such schedule. */
+int hc_batch_set_schedule(hc_batch* b, int dim, int variant);
 
 /* ---- calcDT without allocation ---------------------------------------------
  *

@@ -3,8 +3,9 @@
 // CPU restatement, in plain C++ and double precision, of the finite-volume
 // Euler update that hydro-cl-lua generates from its Lua/OpenCL templates for
 // this option set: Euler equations, Cartesian chart (holonomic vectors,
-// side-permutation normals), numGhost = 2, Roe flux (entropy fix off) with an
-// optional flux limiter, optional "plm cons" reconstruction with a slope
+// side-permutation normals), numGhost = 2, Roe flux (entropy fix off, the
+// fluxFromCons form Euler inherits) with an optional flux limiter, HLL and
+// Rusanov fluxes, optional "plm cons" reconstruction with a slope
 // limiter, the freeflow / periodic / mirror boundaries, the explicit
 // integrators (forward Euler and the Runge-Kutta tables), calcDT and
 // constrainU, and the App's update loop (exit test before stepping, so the
@@ -47,7 +48,8 @@ struct prim_t { real rho; real v[3]; real P; real ePot; };
 struct eigen_t { real rho; real v[3]; real hTotal; real Cs; real vSq; real vL[3]; };
 
 enum { BC_NONE = 0, BC_PERIODIC = 1, BC_MIRROR = 2, BC_FREEFLOW = 3 };
-enum { RECON_NONE = 0, RECON_PIECEWISE_CONSTANT = 1, RECON_PLM_CONS = 2 };
+enum { RECON_NONE = 0, RECON_PIECEWISE_CONSTANT = 1, RECON_PLM_CONS = 2, RECON_PLM_PRIM = 3, RECON_PLM_ATHENA = 4 };
+enum { FLUX_ROE = 0, FLUX_HLL = 1, FLUX_RUSANOV = 2, FLUX_HLLC = 3 };
 
 // OpenCL C max/min on floating types: "returns y if x < y, otherwise x" and
 // "returns y if y < x, otherwise x".
@@ -116,6 +118,8 @@ struct Solver {
 	real mins[3], maxs[3], grid_dx[3];
 	int bc[6];         // xmin xmax ymin ymax zmin zmax
 	int fluxLimiter, recon, slopeLimiter, integrator;
+	int fluxType;      // FLUX_*
+	int hllcMethod;    // euler-hllc's hllcMethod: 0, 1, 2
 	real gamma, rhoMin, PMin, cfl, fixedDT;
 	static const int numGhost = 2;
 
@@ -306,7 +310,23 @@ static void eigen_rightTransform(real result[6], const Solver& s, const eigen_t&
 	result[5] = 0;
 }
 
-// hydro/flux/roe.cl:17-163 (roeUseFluxFromCons unset for Euler, entropy fix off)
+// euler.cl:271-291 (fluxFromCons): F = (rho v_n, m v_n + n P, (ETotal + P) v_n, 0)
+// with n = normal_u1 = e_side for the Cartesian side normals (coord.lua:2378-2386)
+static void fluxFromCons(cons_t& F, const Solver& s, const cons_t& U, int side) {
+	prim_t W;
+	primFromCons(W, s, U);
+	real const v_n = W.v[side];
+	F.ptr[0] = U.ptr[0] * v_n;
+	for (int i = 0; i < 3; ++i) F.ptr[1 + i] = U.ptr[1 + i] * v_n + (side == i ? 1. : 0.) * W.P;
+	real const HTotal = U.ptr[4] + W.P;
+	F.ptr[4] = HTotal * v_n;
+	F.ptr[5] = 0;
+}
+
+// hydro/flux/roe.cl:17-163, entropy fix off, with roeUseFluxFromCons: Euler
+// does not set it and inherits Equation.roeUseFluxFromCons = true
+// (hydro/eqn/eqn.lua:46), so the flux is R.fluxEig + (F(UL) + F(UR)) / 2 with
+// fluxEig_j = 0 - lambda_j dW_j (sgn + phi (lambda_j dt/dx - sgn)) / 2.
 static void roeFluxForInterface(
 	cons_t& resultFlux, const Solver& s,
 	const cons_t& UL, const cons_t& UR, int side, bool useFluxLimiter, real dt_dx,
@@ -317,11 +337,7 @@ static void roeFluxForInterface(
 	real const Cs_nLen = 1. * eig.Cs;
 	real const v_n = eig.v[side];
 
-	real UAvg[6];
-	for (int j = 0; j < 5; ++j) UAvg[j] = .5 * (UL.ptr[j] + UR.ptr[j]);
-	UAvg[5] = 0;
 	real fluxEig[5];
-	eigen_leftTransform(fluxEig, s, eig, UAvg, side);
 
 	real deltaU[6], deltaUL[6], deltaUR[6];
 	for (int j = 0; j < 6; ++j) {
@@ -343,7 +359,7 @@ static void roeFluxForInterface(
 
 	for (int j = 0; j < 5; ++j) {
 		real const lambda = j == 0 ? v_n - Cs_nLen : (j == 4 ? v_n + Cs_nLen : v_n);
-		fluxEig[j] *= lambda;
+		fluxEig[j] = 0.;
 		real const sgnLambda = lambda >= 0 ? 1 : -1;
 		if (useFluxLimiter) {
 			real rEig;
@@ -361,6 +377,164 @@ static void roeFluxForInterface(
 		}
 	}
 	eigen_rightTransform(resultFlux.ptr, s, eig, fluxEig, side);
+	cons_t FL, FR;
+	fluxFromCons(FL, s, UL, side);
+	fluxFromCons(FR, s, UR, side);
+	for (int j = 0; j < 5; ++j) resultFlux.ptr[j] += .5 * (FL.ptr[j] + FR.ptr[j]);
+}
+
+// euler.lua:329-337 (consWaveCodePrefix) with normal_len = 1: the slowest and
+// fastest waves v_n -/+ Cs of one conserved state
+static inline void consWaveMinMax(const Solver& s, const cons_t& U, int side, real& lmin, real& lmax) {
+	real Cs_nLen = calc_Cs_fromCons(s, U);
+	Cs_nLen *= 1.;
+	real const v_n = U.ptr[0] < s.rhoMin ? 0. : U.ptr[1 + side] / U.ptr[0];
+	lmin = v_n - Cs_nLen;
+	lmax = v_n + Cs_nLen;
+}
+
+// OpenCL max / min on reals (x < y ? y : x, y < x ? y : x)
+static inline real clMax(real x, real y) { return x < y ? y : x; }
+static inline real clMin(real x, real y) { return y < x ? y : x; }
+
+// hydro/flux/rusanov.cl: the wave bound lambdaMax is assigned once per side in
+// a loop over L then R, so the right state's value is the one used.
+static void rusanovFluxForInterface(cons_t& resultFlux, const Solver& s, const cons_t& UL, const cons_t& UR, int side) {
+	real lambdaMax = 0;
+	{
+		real lmin, lmax;
+		consWaveMinMax(s, UL, side, lmin, lmax);
+		lambdaMax = clMax(std::fabs(lmin), std::fabs(lmax));
+	}
+	{
+		real lmin, lmax;
+		consWaveMinMax(s, UR, side, lmin, lmax);
+		lambdaMax = clMax(std::fabs(lmin), std::fabs(lmax));
+	}
+	cons_t FL, FR;
+	fluxFromCons(FL, s, UL, side);
+	fluxFromCons(FR, s, UR, side);
+	for (int j = 0; j < 5; ++j)
+		resultFlux.ptr[j] = .5 * (FL.ptr[j] + FR.ptr[j] - lambdaMax * (UR.ptr[j] - UL.ptr[j]));
+}
+
+// hydro/flux/hll.cl with hllCalcWaveMethod = 'Davis direct bounded' (hll.lua:9):
+// sL = min(v_n - Cs of UL, Roe-average v_n - Cs), sR = max(v_n + Cs of UR,
+// Roe-average v_n + Cs).  When sL or sR is NaN no branch assigns the flux and
+// the flux buffer keeps its previous content, as in the reference.
+static void hllFluxForInterface(cons_t& resultFlux, const Solver& s, const cons_t& UL, const cons_t& UR, int side) {
+	eigen_t eigInt;
+	eigen_forInterface(eigInt, s, UL, UR);
+	real const Cs_nLen = 1. * eigInt.Cs;
+	real const v_n = eigInt.v[side];
+	real const lambdaIntMin = v_n - Cs_nLen;
+	real const lambdaIntMax = v_n + Cs_nLen;
+	real lambdaLMin, lambdaRMax, unused;
+	consWaveMinMax(s, UL, side, lambdaLMin, unused);
+	consWaveMinMax(s, UR, side, unused, lambdaRMax);
+	real const sL = clMin(lambdaLMin, lambdaIntMin);
+	real const sR = clMax(lambdaRMax, lambdaIntMax);
+	if (0 <= sL) {
+		fluxFromCons(resultFlux, s, UL, side);
+	} else if (sR <= 0) {
+		fluxFromCons(resultFlux, s, UR, side);
+	} else if (sL <= 0 && 0 <= sR) {
+		cons_t FL, FR;
+		fluxFromCons(FL, s, UL, side);
+		fluxFromCons(FR, s, UR, side);
+		for (int j = 0; j < 5; ++j)
+			resultFlux.ptr[j] = (sR * FL.ptr[j] - sL * FR.ptr[j] + sL * sR * (UR.ptr[j] - UL.ptr[j])) / (sR - sL);
+	}
+}
+
+// hydro/flux/euler-hllc.cl (2012 Toro's HLLC, hllcMethod 0 / 1 / 2; waves
+// as hll.cl's 'Davis direct bounded').  Vectors in the interface frame:
+// vn = normal_vecDotNs(n, v) = (v[side], v[side+1], v[side+2]); back to
+// the global frame with normal_vecFromNs (coord.lua:2392-2407).
+static inline void vecFromNs(real out[3], int side, const real v[3]) {
+	for (int i = 0; i < 3; ++i) out[i] = v[(3 - side + i) % 3];
+}
+static void hllcFluxForInterface(cons_t& flux, const Solver& s, const cons_t& UL, const cons_t& UR, int side) {
+	prim_t WL, WR;
+	primFromCons(WL, s, UL);
+	primFromCons(WR, s, UR);
+	eigen_t eigInt;
+	eigen_forInterface(eigInt, s, UL, UR);
+	real const Cs_nLen = 1. * eigInt.Cs;
+	real const v_n = eigInt.v[side];
+	real const lambdaIntMin = v_n - Cs_nLen;
+	real const lambdaIntMax = v_n + Cs_nLen;
+	real lambdaLMin, lambdaRMax, unused;
+	consWaveMinMax(s, UL, side, lambdaLMin, unused);
+	consWaveMinMax(s, UR, side, unused, lambdaRMax);
+	real const sL = clMin(lambdaLMin, lambdaIntMin);
+	real const sR = clMax(lambdaRMax, lambdaIntMax);
+	real const vnL[3] = {WL.v[side], WL.v[(side + 1) % 3], WL.v[(side + 2) % 3]};
+	real const vnR[3] = {WR.v[side], WR.v[(side + 1) % 3], WR.v[(side + 2) % 3]};
+	real const sStar = (WR.rho * vnR[0] * (sR - vnR[0]) - WL.rho * vnL[0] * (sL - vnL[0]) + WL.P - WR.P)
+		/ (WR.rho * (sR - vnR[0]) - WL.rho * (sL - vnL[0]));
+	int const m = s.hllcMethod;
+	// one side of the star region: X = L (sgn 0) or R
+	auto star = [&](const cons_t& U, const prim_t& W, const real* vn, real sK) {
+		cons_t F;
+		fluxFromCons(F, s, U, side);
+		if (m == 0) {
+			cons_t UStar;
+			UStar.ptr[0] = U.ptr[0] * (sK - vn[0]) / (sK - sStar);
+			real const vs[3] = {sStar, vn[1], vn[2]};
+			real vStar[3];
+			vecFromNs(vStar, side, vs);
+			for (int i = 0; i < 3; ++i) UStar.ptr[1 + i] = UStar.ptr[0] * vStar[i];
+			UStar.ptr[4] = UStar.ptr[0] * (U.ptr[4] / U.ptr[0] + (sStar - vn[0]) * (sStar + W.P / (U.ptr[0] * (sK - vn[0]))));
+			UStar.ptr[5] = U.ptr[5];   // never set by the reference; its flux is not used
+			for (int i = 0; i < 6; ++i) flux.ptr[i] = F.ptr[i] + sK * (UStar.ptr[i] - U.ptr[i]);
+			return;
+		}
+		real const Umn[3] = {U.ptr[1 + side], U.ptr[1 + (side + 1) % 3], U.ptr[1 + (side + 2) % 3]};
+		real const Fmn[3] = {F.ptr[1 + side], F.ptr[1 + (side + 1) % 3], F.ptr[1 + (side + 2) % 3]};
+		real mflux[3], out[3];
+		if (m == 1) {
+			flux.ptr[0] = (sStar * (sK * U.ptr[0] - F.ptr[0])) / (sK - sStar);
+			mflux[0] = (sStar * (sK * Umn[0] - Fmn[0]) + sK * (W.P + W.rho * (sK - vn[0]) * (sStar - vn[0]))) / (sK - sStar);
+			mflux[1] = (sStar * (sK * Umn[1] - Fmn[1])) / (sK - sStar);
+			mflux[2] = (sStar * (sK * Umn[2] - Fmn[2])) / (sK - sStar);
+			vecFromNs(out, side, mflux);
+			for (int i = 0; i < 3; ++i) flux.ptr[1 + i] = out[i];
+			flux.ptr[4] = (sStar * (sK * U.ptr[4] - F.ptr[4]) + sK * (W.P + W.rho * (sK - vn[0]) * (sStar - vn[0])) * sStar) / (sK - sStar);
+		} else {
+			real const PLR = .5 * (WL.P + WR.P + WL.rho * (sL - vnL[0]) * (sStar - vnL[0]) + WR.rho * (sR - vnR[0]) * (sStar - vnR[0]));
+			// the left branch writes (sL rho - F rho) sStar / (..), the right one sStar (sR rho - F rho) / (..)
+			if (&U == &UL) flux.ptr[0] = (sK * U.ptr[0] - F.ptr[0]) * sStar / (sK - sStar);
+			else flux.ptr[0] = sStar * (sK * U.ptr[0] - F.ptr[0]) / (sK - sStar);
+			mflux[0] = ((sK * Umn[0] - Fmn[0]) * sStar + sK * PLR) / (sK - sStar);
+			if (&U == &UL) {
+				mflux[1] = sStar * (sK * Umn[1] - Fmn[1]) / (sK - sStar);
+				mflux[2] = sStar * (sK * Umn[2] - Fmn[2]) / (sK - sStar);
+			} else {
+				mflux[0] = (sStar * (sK * Umn[0] - Fmn[0]) + sK * PLR) / (sK - sStar);
+				mflux[1] = sStar * (sK * Umn[1] - Fmn[1]) / (sK - sStar);
+				mflux[2] = sStar * (sK * Umn[2] - Fmn[2]) / (sK - sStar);
+			}
+			vecFromNs(out, side, mflux);
+			for (int i = 0; i < 3; ++i) flux.ptr[1 + i] = out[i];
+			flux.ptr[4] = (sStar * (sK * U.ptr[4] - F.ptr[4]) + sK * PLR * sStar) / (sK - sStar);
+		}
+	};
+	if (0 <= sL) {
+		fluxFromCons(flux, s, UL, side);
+	} else if (sL <= 0. && 0. <= sStar) {
+		star(UL, WL, vnL, sL);
+	} else if (sStar <= 0. && 0. <= sR) {
+		star(UR, WR, vnR, sR);
+	} else if (sR <= 0) {
+		fluxFromCons(flux, s, UR, side);
+	} else if (sL <= 0 && 0 <= sR) {
+		cons_t FL, FR;
+		fluxFromCons(FL, s, UL, side);
+		fluxFromCons(FR, s, UR, side);
+		for (int j = 0; j < 5; ++j)
+			flux.ptr[j] = (sR * FL.ptr[j] - sL * FR.ptr[j] + sL * sR * (UR.ptr[j] - UL.ptr[j])) / (sR - sL);
+	}
 }
 
 // ---------------------------------------------------------------------------
@@ -447,7 +621,143 @@ static void constrainU(Solver& s) {
 	boundary(s);
 }
 
-// hydro/solver/plm.cl:27-91, 976-997 ("plm cons", "piecewise constant")
+// OpenCL C sign(): 1 for x > 0, -1 for x < 0, x itself for +-0, 0 for NaN.
+static inline real clSign(real x) { return x > 0 ? 1. : (x < 0 ? -1. : (x == 0 ? x : 0.)); }
+
+static inline real& primAt(prim_t& W, int j) { return j == 0 ? W.rho : (j < 4 ? W.v[j - 1] : (j == 4 ? W.P : W.ePot)); }
+
+// "plm cons", hydro/solver/plm.cl:27-91
+static void plmCons(cons_t& L, cons_t& R, const Solver& s, const cons_t& UL, const cons_t& U, const cons_t& UR) {
+	L = U;
+	R = U;
+	for (int j = 0; j < 5; ++j) {
+		real const dUR = UR.ptr[j] - U.ptr[j];
+		real const dUL = U.ptr[j] - UL.ptr[j];
+		real sigma;
+		real const dUC = .5 * (dUR - dUL);
+		if (dUC >= 0) {
+			real const r = dUR == 0 ? 0 : (dUL / dUR);
+			real const phi = limiter(s.slopeLimiter, r);
+			sigma = phi * dUR;
+		} else {
+			real const r = dUL == 0 ? 0 : (dUR / dUL);
+			real const phi = limiter(s.slopeLimiter, r);
+			sigma = phi * dUL;
+		}
+		R.ptr[j] += .5 * sigma;
+		L.ptr[j] -= .5 * sigma;
+	}
+}
+
+// "plm prim", hydro/solver/plm.cl:191-253: slopes of the primitives,
+// r = dWL / dWR, sigma = phi(r) dWR
+static void plmPrim(cons_t& L, cons_t& R, const Solver& s, const cons_t& UL, const cons_t& U, const cons_t& UR) {
+	prim_t W, WL, WR;
+	primFromCons(W, s, U);
+	primFromCons(WL, s, UL);
+	primFromCons(WR, s, UR);
+	prim_t nWL = W, nWR = W;
+	for (int j = 0; j < 5; ++j) {
+		real const dWR = primAt(WR, j) - primAt(W, j);
+		real const dWL = primAt(W, j) - primAt(WL, j);
+		real const r = dWR == 0 ? 0 : (dWL / dWR);
+		real const phi = limiter(s.slopeLimiter, r);
+		real const sigma = phi * dWR;
+		primAt(nWL, j) -= .5 * sigma;
+		primAt(nWR, j) += .5 * sigma;
+	}
+	consFromPrim(L, s, nWL);
+	consFromPrim(R, s, nWR);
+}
+
+// eigen_forCell, hydro/eqn/euler.cl:315-342
+static void eigen_forCell(eigen_t& e, const Solver& s, const cons_t& U) {
+	prim_t W;
+	primFromCons(W, s, U);
+	real vL[3] = { W.v[0], W.v[1], W.v[2] };
+	real const vSq = real3_dot(W.v, vL);
+	real const eKin = .5 * vSq;
+	real const hTotal = calc_hTotal(W.rho, W.P, U.ptr[4]);
+	real const CsSq = (s.gamma - 1.) * (hTotal - eKin);
+	real const Cs = std::sqrt(CsSq);
+	e.rho = W.rho;
+	for (int k = 0; k < 3; ++k) { e.v[k] = W.v[k]; e.vL[k] = vL[k]; }
+	e.vSq = vSq;
+	e.hTotal = hTotal;
+	e.Cs = Cs;
+}
+
+// The edge assignment of the revision that recorded the reference's 'plm-athena'
+// errors (tests/test-order/schemes.lua:104,117-126): L from the left-edge
+// value, R from the right-edge value.  With it the oracle reproduces those
+// recorded errors; the current source (the default, 0) swaps the two.
+static int g_plmAthenaRecordedEdges = 0;
+
+// "plm athena", the first of the two branches of that name
+// (hydro/solver/plm.cl:782-879; the second, :950-968, is never reached): the
+// primitive differences are projected with the cell's eigenvectors of the
+// conserved system, limited per wave, projected back, clamped to the
+// neighbouring primitives, and stored with the reference's assignment: the
+// cell's L state from the right-edge value and its R state from the
+// left-edge value (plm.cl:877-878) unless g_plmAthenaRecordedEdges is set.
+static void plmAthena(cons_t& L, cons_t& R, const Solver& s, const cons_t& UL, const cons_t& U, const cons_t& UR,
+		int side) {
+	eigen_t eig;
+	eigen_forCell(eig, s, U);
+	prim_t W, WL, WR;
+	primFromCons(W, s, U);
+	primFromCons(WL, s, UL);
+	primFromCons(WR, s, UR);
+	real dWL[6], dWR[6], dWC[6], dWG[6];
+	for (int j = 0; j < 5; ++j) {
+		dWL[j] = primAt(W, j) - primAt(WL, j);
+		dWR[j] = primAt(WR, j) - primAt(W, j);
+		dWC[j] = .5 * (primAt(WR, j) - primAt(WL, j));
+		dWG[j] = (dWL[j] * dWR[j]) <= 0. ? 0. : (2. * dWL[j] * dWR[j] / (dWL[j] + dWR[j]));
+	}
+	dWL[5] = dWR[5] = dWC[5] = dWG[5] = 0.;
+	real dal[5], dar[5], dac[5], dag[5];
+	eigen_leftTransform(dal, s, eig, dWL, side);
+	eigen_leftTransform(dar, s, eig, dWR, side);
+	eigen_leftTransform(dac, s, eig, dWC, side);
+	eigen_leftTransform(dag, s, eig, dWG, side);
+	real da[5];
+	for (int j = 0; j < 5; ++j) {
+		da[j] = 0;
+		if (dal[j] * dar[j] > 0) {
+			real const lim_slope1 = clMin(std::fabs(dal[j]), std::fabs(dar[j]));
+			real const lim_slope2 = clMin(std::fabs(dac[j]), std::fabs(dag[j]));
+			da[j] = clSign(dac[j]) * clMin((real)2. * lim_slope1, lim_slope2);
+		}
+	}
+	real dWm[6];
+	eigen_rightTransform(dWm, s, eig, da, side);
+	prim_t Wlv = W, Wrv = W;
+	for (int j = 0; j < 5; ++j) {
+		real const w = primAt(W, j), wl = primAt(WL, j), wr = primAt(WR, j);
+		real lv = w - .5 * dWm[j];
+		real rv = w + .5 * dWm[j];
+		real const C = rv + lv;
+		lv = clMax(clMin(w, wl), lv);
+		lv = clMin(clMax(w, wl), lv);
+		rv = C - lv;
+		rv = clMax(clMin(w, wr), rv);
+		rv = clMin(clMax(w, wr), rv);
+		lv = C - rv;
+		primAt(Wlv, j) = lv;
+		primAt(Wrv, j) = rv;
+	}
+	if (g_plmAthenaRecordedEdges) {
+		consFromPrim(L, s, Wlv);
+		consFromPrim(R, s, Wrv);
+	} else {
+		consFromPrim(L, s, Wrv);
+		consFromPrim(R, s, Wlv);
+	}
+}
+
+// hydro/solver/plm.cl:976-997 (calcLR over [1, n-1) on every axis);
+// "piecewise constant" copies the cell (plm.cl:10-25)
 static void calcLR(Solver& s) {
 	forAllCells(s, [&](const int* i, long index) {
 		if (OOB(s, i, 1, 1)) return;
@@ -455,27 +765,13 @@ static void calcLR(Solver& s) {
 		for (int side = 0; side < s.dim; ++side) {
 			cons_t& L = s.ULR[2 * (side + s.dim * index) + 0];
 			cons_t& R = s.ULR[2 * (side + s.dim * index) + 1];
-			L = U;
-			R = U;
-			if (s.recon != RECON_PLM_CONS) continue;
 			const cons_t& UL = s.U[index - s.stepsize[side]];
 			const cons_t& UR = s.U[index + s.stepsize[side]];
-			for (int j = 0; j < 5; ++j) {
-				real const dUR = UR.ptr[j] - U.ptr[j];
-				real const dUL = U.ptr[j] - UL.ptr[j];
-				real sigma;
-				real const dUC = .5 * (dUR - dUL);
-				if (dUC >= 0) {
-					real const r = dUR == 0 ? 0 : (dUL / dUR);
-					real const phi = limiter(s.slopeLimiter, r);
-					sigma = phi * dUR;
-				} else {
-					real const r = dUL == 0 ? 0 : (dUR / dUL);
-					real const phi = limiter(s.slopeLimiter, r);
-					sigma = phi * dUL;
-				}
-				R.ptr[j] += .5 * sigma;
-				L.ptr[j] -= .5 * sigma;
+			switch (s.recon) {
+			case RECON_PLM_CONS: plmCons(L, R, s, UL, U, UR); break;
+			case RECON_PLM_PRIM: plmPrim(L, R, s, UL, U, UR); break;
+			case RECON_PLM_ATHENA: plmAthena(L, R, s, UL, U, UR, side); break;
+			default: L = U; R = U; break;
 			}
 		}
 	});
@@ -485,7 +781,8 @@ static void calcLR(Solver& s) {
 static void calcFlux(Solver& s, real dt) {
 	int const G = Solver::numGhost;
 	bool const usePLM = s.recon != RECON_NONE;
-	bool const useFluxLimiter = s.fluxLimiter > 0;
+	// only the Roe flux takes the flux limiter (fvsolver.lua:62-64, flux.usesFluxLimiter)
+	bool const useFluxLimiter = s.fluxLimiter > 0 && s.fluxType == FLUX_ROE;
 	forAllCells(s, [&](const int* i, long index) {
 		if (OOB(s, i, G, G - 1)) return;
 		long const indexR = index;
@@ -518,7 +815,10 @@ static void calcFlux(Solver& s, real dt) {
 				lr(indexL2, indexL, UL_L, UR_L);
 				lr(indexR, indexR2, UL_R, UR_R);
 			}
-			roeFluxForInterface(flux, s, *UL, *UR, side, useFluxLimiter, dt_dx, UL_L, UL_R, UR_L, UR_R);
+			if (s.fluxType == FLUX_HLL) hllFluxForInterface(flux, s, *UL, *UR, side);
+			else if (s.fluxType == FLUX_HLLC) hllcFluxForInterface(flux, s, *UL, *UR, side);
+			else if (s.fluxType == FLUX_RUSANOV) rusanovFluxForInterface(flux, s, *UL, *UR, side);
+			else roeFluxForInterface(flux, s, *UL, *UR, side, useFluxLimiter, dt_dx, UL_L, UL_R, UR_L, UR_R);
 		}
 	});
 }
@@ -680,6 +980,8 @@ typedef struct or_desc {
 	double p_min;
 	double cfl;
 	double fixed_dt;
+	int flux;          // FLUX_*: roe, hll, rusanov, euler-hllc
+	int hllc_method;   // 0: the reference's default (its hllcMethod 2); 1, 2, 3: its hllcMethod 0, 1, 2
 } or_desc;
 
 void* or_create(const or_desc* d) {
@@ -699,6 +1001,8 @@ void* or_create(const or_desc* d) {
 	s->numCells = (long)s->gs[0] * s->gs[1] * s->gs[2];
 	for (int k = 0; k < 6; ++k) s->bc[k] = d->boundary[k];
 	s->fluxLimiter = d->flux_limiter;
+	s->fluxType = d->flux;
+	s->hllcMethod = d->hllc_method == 0 ? 2 : d->hllc_method - 1;
 	s->recon = d->recon;
 	s->slopeLimiter = d->slope_limiter;
 	s->integrator = d->integrator;
@@ -792,6 +1096,21 @@ void or_get_flux(void* h, double* dst) {
 }
 
 // Single-interface Roe flux, for unit checks.
+// The interface flux of the descriptor's flux function (roe without a limiter, hll, rusanov).
+void or_interface_flux(const or_desc* d, const double* UL, const double* UR, int side, double* out) {
+	Solver* s = (Solver*)or_create(d);
+	cons_t a, b, f;
+	std::memcpy(a.ptr, UL, sizeof(a));
+	std::memcpy(b.ptr, UR, sizeof(b));
+	std::memset(f.ptr, 0, sizeof(f));
+	if (d->flux == FLUX_HLL) hllFluxForInterface(f, *s, a, b, side);
+	else if (d->flux == FLUX_HLLC) hllcFluxForInterface(f, *s, a, b, side);
+	else if (d->flux == FLUX_RUSANOV) rusanovFluxForInterface(f, *s, a, b, side);
+	else roeFluxForInterface(f, *s, a, b, side, false, 0, 0, 0, 0, 0);
+	std::memcpy(out, f.ptr, sizeof(f));
+	delete s;
+}
+
 void or_roe_flux(const or_desc* d, const double* UL, const double* UR, int side, double* out) {
 	Solver* s = (Solver*)or_create(d);
 	cons_t a, b, f;
@@ -832,6 +1151,9 @@ void or_eigen_basis(const or_desc* d, const double* UL, const double* UR, int si
 }
 
 double or_limiter(int which, double r) { return limiter(which, r); }
+
+// 1: "plm athena" with the recorded revision's edge assignment; 0: the current source's
+void or_set_plm_athena_recorded_edges(int on) { g_plmAthenaRecordedEdges = on ? 1 : 0; }
 
 int or_num_threads(void) {
 #ifdef _OPENMP

@@ -41,7 +41,7 @@ INTEGRATORS = [
     "Runge-Kutta 4, non-TVD",
 ]
 BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3}
-RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2}
+RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2, "plm prim": 3, "plm athena": 4}
 
 
 def build(force=False):
@@ -73,7 +73,12 @@ class OrDesc(ctypes.Structure):
         ("p_min", ctypes.c_double),
         ("cfl", ctypes.c_double),
         ("fixed_dt", ctypes.c_double),
+        ("flux", ctypes.c_int),
+        ("hllc_method", ctypes.c_int),
     ]
+
+# flux names in the reference's vocabulary (hydro/flux/*.lua)
+FLUXES = ["roe", "hll", "rusanov", "euler-hllc"]
 
 
 _lib = None
@@ -107,10 +112,12 @@ def lib():
         L.or_calc_deriv.argtypes = [vp, ctypes.c_double, dp]
         L.or_get_flux.argtypes = [vp, dp]
         L.or_roe_flux.argtypes = [ctypes.POINTER(OrDesc), dp, dp, ip, dp]
+        L.or_interface_flux.argtypes = [ctypes.POINTER(OrDesc), dp, dp, ip, dp]
         L.or_eigen_basis.argtypes = [ctypes.POINTER(OrDesc), dp, dp, ip, dp, dp, dp]
         L.or_limiter.restype = ctypes.c_double
         L.or_limiter.argtypes = [ip, ctypes.c_double]
         L.or_num_threads.restype = ctypes.c_int
+        L.or_set_plm_athena_recorded_edges.argtypes = [ip]
         _lib = L
     return _lib
 
@@ -148,6 +155,9 @@ def make_desc(cfg):
     d.p_min = float(eq.get("PMin", 1e-7))
     d.cfl = float(cfg.get("cfl", 0.5))
     d.fixed_dt = float(cfg.get("fixedDT", 0.0) or 0.0)
+    d.flux = FLUXES.index(cfg.get("flux", "roe"))
+    # euler-hllc's hllcMethod (default 2, euler-hllc.lua:19); 0 in the descriptor is that default
+    d.hllc_method = int(cfg["hllcMethod"]) + 1 if "hllcMethod" in cfg else 0
     return d
 
 
@@ -235,6 +245,16 @@ def roe_flux(cfg, UL, UR, side):
     return out
 
 
+def interface_flux(cfg, UL, UR, side):
+    """The interface flux of cfg["flux"] (roe without a limiter, hll, rusanov)."""
+    d = make_desc(cfg)
+    a = np.ascontiguousarray(UL, dtype=np.float64)
+    b = np.ascontiguousarray(UR, dtype=np.float64)
+    out = np.empty(6)
+    lib().or_interface_flux(ctypes.byref(d), _ptr(a), _ptr(b), int(side), _ptr(out))
+    return out
+
+
 def eigen_basis(cfg, UL, UR, side):
     d = make_desc(cfg)
     a = np.ascontiguousarray(UL, dtype=np.float64)
@@ -249,6 +269,21 @@ def eigen_basis(cfg, UL, UR, side):
 def limiter(name_or_index, r):
     idx = LIMITERS.index(name_or_index) if isinstance(name_or_index, str) else int(name_or_index)
     return lib().or_limiter(idx, float(r))
+
+
+class plm_athena_recorded_edges:
+    """Within this context "plm athena" assigns the cell's L state from its
+    left-edge value and R from its right-edge value, as the revision that
+    recorded the reference's 'plm-athena' errors did; outside it the oracle
+    follows the current source, which swaps the two (plm.cl:877-878)."""
+
+    def __enter__(self):
+        lib().or_set_plm_athena_recorded_edges(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().or_set_plm_athena_recorded_edges(0)
+        return False
 
 
 def num_threads():

@@ -75,8 +75,14 @@ def test_descriptor_mapping_follows_reference_names():
     assert d.flux_limiter == 18 and d.integrator == 9 and abs(d.gamma - 5 / 3) < 1e-15
     with pytest.raises(ValueError):
         hydrocuda.make_desc(dict(dim=1, gridSize=8, fluxLimiter="no such limiter"))
+    assert hydrocuda.make_desc(dict(dim=1, gridSize=8, flux="hll")).flux == 1
+    assert hydrocuda.make_desc(dict(dim=1, gridSize=8, flux="rusanov")).flux == 2
     with pytest.raises(ValueError):
-        hydrocuda.make_desc(dict(dim=1, gridSize=8, flux="hll"))
+        hydrocuda.make_desc(dict(dim=1, gridSize=8, flux="marquina"))
+    assert hydrocuda.make_desc(dict(dim=1, gridSize=8, usePLM="plm prim")).recon == 3
+    assert hydrocuda.make_desc(dict(dim=1, gridSize=8, usePLM="plm athena")).recon == 4
+    with pytest.raises(ValueError):
+        hydrocuda.make_desc(dict(dim=1, gridSize=8, usePLM="ppm"))
 
 
 def test_init_defaults_without_a_device():

@@ -118,8 +118,11 @@ template <typename V> struct Eig {
 // The Roe average with both sides above the vacuum threshold
 // (euler.cl:347-430): one reciprocal square root per side gives
 // sqrt(rho) = rho rs, 1/rho = rs^2 and the Roe weights.
+// Also returns the left side's pressure and 1/rho, and the lanes where the
+// enthalpy fell below its threshold (hTotal and Cs replaced).
 template <typename V>
-__device__ __forceinline__ V eigenRoe(Eig<V>& e, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+__device__ __forceinline__ V eigenRoe(Eig<V>& e, const Eos& s, const C5<V>& UL, const C5<V>& UR, V& PLout, V& invLout,
+                                      Mask<V>& lowOut) {
     V const half = splat<V>(.5f), nhalf = splat<V>(-.5f), g1 = splat<V>(s.g1), rhoMin = splat<V>(s.rhoMin),
             zero = splat<V>(0.f);
     V const rsL = rsq(UL.u[0]), rsR = rsq(UR.u[0]);
@@ -140,7 +143,17 @@ __device__ __forceinline__ V eigenRoe(Eig<V>& e, const Eos& s, const C5<V>& UL, 
     auto const low = lt(h, splat<V>(1e-5f));
     e.hT = sel(low, eKin, hT);
     e.Cs = sel(low, zero, sqr(mul(g1, h)));
+    PLout = PL;
+    invLout = invL;
+    lowOut = low;
     return mul(sL, sR);   // the averaged density
+}
+
+template <typename V>
+__device__ __forceinline__ V eigenRoe(Eig<V>& e, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+    V PL, invL;
+    Mask<V> low;
+    return eigenRoe(e, s, UL, UR, PL, invL, low);
 }
 
 // One side at the vacuum threshold (or both): the other side's state, or zero.
@@ -339,7 +352,7 @@ __device__ __forceinline__ void hll(V* F, const Eos& s, const C5<V>& UL, const C
 // Euler inherits (roeUseFluxFromCons, eqn.lua:46):
 //   F = (F(UL) + F(UR)) / 2 - R |Lambda| L.(UR - UL) / 2.
 template <typename V>
-__device__ __forceinline__ void roe(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+__device__ __forceinline__ void roeCentral(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
     Eig<V> e;
     eigen(e, s, UL, UR);
     V dU[5], dW[5], fe[5];
@@ -362,6 +375,55 @@ __device__ __forceinline__ void roe(V* F, const Eos& s, const C5<V>& UL, const C
     V const half = splat<V>(.5f);
 #pragma unroll
     for (int j = 0; j < 5; ++j) F[j] = fma(half, add(FL[j], FR[j]), F[j]);
+}
+
+// With the plain Roe average (both densities above the vacuum threshold,
+// the enthalpy above its floor, the averaged density at least rhoMin) the
+// Roe matrix has property U, F(UR) - F(UL) = R Lambda L.(UR - UL), and the
+// flux above equals the upwind form F(UL) + R min(Lambda, 0) L.(UR - UL):
+// one physical flux instead of two, built from the left side's pressure and
+// 1/rho that the average already has.  Other states take the form above.
+template <typename V>
+__device__ __forceinline__ void roe(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+    if constexpr (nlanes<V>() == 1) {
+        bool const lv = UL.u[0] < 1e-5f, rv = UR.u[0] < 1e-5f;
+        Eig<float> e;
+        float PL = 0.f, invL = 0.f;
+        bool low = false;
+        float const rho = (lv || rv) ? eigenVac(e, s, UL, UR, lv, rv) : eigenRoe(e, s, UL, UR, PL, invL, low);
+        finishEig(e, s, rho);
+        bool const pu = !(lv || rv || low || e.ident);
+        float dU[5], dW[5], fe[5];
+#pragma unroll
+        for (int j = 0; j < 5; ++j) dU[j] = sub(UR.u[j], UL.u[j]);
+        left(dW, e, s, dU);
+        float const l0 = sub(e.vn, e.Cs), l4 = add(e.vn, e.Cs);
+        float const c0 = pu ? vmin(l0, 0.f) : mul(-.5f, absv(l0));
+        float const c1 = pu ? vmin(e.vn, 0.f) : mul(-.5f, absv(e.vn));
+        float const c4 = pu ? vmin(l4, 0.f) : mul(-.5f, absv(l4));
+        fe[0] = mul(c0, dW[0]);
+        fe[1] = mul(c1, dW[1]);
+        fe[2] = mul(c1, dW[2]);
+        fe[3] = mul(c1, dW[3]);
+        fe[4] = mul(c4, dW[4]);
+        right(F, e, fe);
+        if (pu) {
+            float const vn = mul(UL.u[1], invL);
+            F[0] = add(F[0], UL.u[1]);
+            F[1] = add(F[1], fma(UL.u[1], vn, PL));
+            F[2] = fma(UL.u[2], vn, F[2]);
+            F[3] = fma(UL.u[3], vn, F[3]);
+            F[4] = fma(add(UL.u[4], PL), vn, F[4]);
+        } else {
+            float FL[5], FR[5], PLc, PRc;
+            fluxOf(FL, PLc, s, UL);
+            fluxOf(FR, PRc, s, UR);
+#pragma unroll
+            for (int j = 0; j < 5; ++j) F[j] = fma(.5f, add(FL[j], FR[j]), F[j]);
+        }
+    } else {
+        roeCentral<V>(F, s, UL, UR);
+    }
 }
 
 // HLLC flux (hydro/flux/euler-hllc.cl, 2012 Toro; waves as hll) in the

@@ -28,6 +28,7 @@ SOURCES = {
     "hc_plan.cu": [],
     "hc_plain.cu": EXACT,
     "hc_init.cu": EXACT,
+    "hc_viz.cu": EXACT,
     "hc_fused_host.cu": [],
     "hc_fused_f32_d1.cu": FAST,
     "hc_fused_f32_d2a.cu": FAST,

@@ -305,6 +305,95 @@ int hc_solver_get_state(hc_solver* s, void* cons, int layout, int with_ghosts) {
     return fused_get_state(s->fused, 0, cons, layout);
 }
 
+// ---- headless visualisation ---------------------------------------------------
+
+// The solver's interior state as AoS-6 FP64 on the device: the plain form's
+// UBuf in place, the fused forms through a scratch copy (*scratch, freed by
+// the caller).
+static int viz_state(hc_solver* s, VizState& st, void** scratch) {
+    *scratch = nullptr;
+    st.d = s->d;
+    long long n[3], f[3];
+    for (int k = 0; k < 3; ++k) {
+        n[k] = k < s->d.dim ? s->d.n[k] : 1;
+        f[k] = k < s->d.dim ? n[k] + 4 : 1;
+    }
+    if (s->plain) {
+        st.stride[0] = 1;
+        st.stride[1] = f[0];
+        st.stride[2] = f[0] * f[1];
+        long long off = 0;
+        for (int k = 0; k < s->d.dim; ++k) off += 2 * st.stride[k];
+        st.U = plain_state_dev(s->plain) + 6 * off;
+        return HC_OK;
+    }
+    HC_CUDA(cudaMalloc(scratch, (size_t)interior_cells(s->d) * 6 * sizeof(double)));
+    st.U = static_cast<const double*>(*scratch);
+    st.stride[0] = 1;
+    st.stride[1] = n[0];
+    st.stride[2] = n[0] * n[1];
+    return fused_get_state_dev(s->fused, 0, *scratch, HC_LAYOUT_AOS6_F64);
+}
+
+int hc_solver_display(hc_solver* s, int var, int zero_border, double* out) {
+    if (!s || !out) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(s->ctx));
+    VizState st;
+    void* scratch = nullptr;
+    double* dev = nullptr;
+    size_t const bytes = (size_t)full_cells(s->d) * sizeof(double);
+    int r = viz_state(s, st, &scratch);
+    if (r == HC_OK) {
+        cudaError_t e = cudaMalloc(&dev, bytes);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMalloc");
+    }
+    if (r == HC_OK) r = viz_display(st, var, zero_border, dev, s->ctx->stream);
+    if (r == HC_OK) {
+        cudaError_t e = cudaMemcpyAsync(out, dev, bytes, cudaMemcpyDeviceToHost, s->ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync");
+    }
+    cudaFree(dev);
+    cudaFree(scratch);
+    return r;
+}
+
+int hc_solver_display_range(hc_solver* s, int var, double out[4]) {
+    if (!s || !out) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(s->ctx));
+    VizState st;
+    void* scratch = nullptr;
+    int r = viz_state(s, st, &scratch);
+    if (r == HC_OK) r = viz_range(st, var, out, s->ctx->stream);
+    cudaFree(scratch);
+    return r;
+}
+
+int hc_solver_render(hc_solver* s, const hc_render* rr, unsigned char* rgba) {
+    if (!s || !rr || !rgba) return fail(HC_ERR_INVALID, "NULL argument");
+    if (rr->width <= 0 || rr->height <= 0 || (long long)rr->width * rr->height > (1ll << 28))
+        return fail(HC_ERR_INVALID, "image size");
+    HC_CHECK(use_device(s->ctx));
+    VizState st;
+    void* scratch = nullptr;
+    void* img = nullptr;
+    size_t const bytes = (size_t)rr->width * rr->height * 4;
+    int r = viz_state(s, st, &scratch);
+    if (r == HC_OK) {
+        cudaError_t e = cudaMalloc(&img, bytes);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMalloc");
+    }
+    if (r == HC_OK) r = viz_render(st, *rr, static_cast<unsigned char*>(img), s->ctx->stream);
+    if (r == HC_OK) {
+        cudaError_t e = cudaMemcpyAsync(rgba, img, bytes, cudaMemcpyDeviceToHost, s->ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);
+        if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync");
+    }
+    cudaFree(img);
+    cudaFree(scratch);
+    return r;
+}
+
 int hc_solver_boundary(hc_solver* s) {
     if (!s) return fail(HC_ERR_INVALID, "NULL solver");
     HC_CHECK(use_device(s->ctx));

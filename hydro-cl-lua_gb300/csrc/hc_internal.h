@@ -105,6 +105,7 @@ int plain_calc_dt(PlainSolver* p, double cfl, double fixed_dt, double* dt);
 int plain_step(PlainSolver* p, int integrator, double dt);
 int plain_conservation(PlainSolver* p, double sums[5]);
 long long plain_num_cells(const PlainSolver* p);
+const double* plain_state_dev(const PlainSolver* p);   // UBuf (AoS-6 FP64, ghosts included) on the device
 
 // ---------------------------------------------------------------------------
 // fused form (hc_fused.cu): a set of instances advanced together
@@ -135,6 +136,17 @@ int plain_init_state(PlainSolver* p, const hc_init& ic, const hc_solver_desc& d)
 int plain_expand_full(const hc_solver_desc& d, const void* interior_dev, int layout, double* full_dev, cudaStream_t s);
 // the slot's interior state into device memory (layout as for host I/O)
 int fused_get_state_dev(FusedSet* f, int slot, void* dev, int layout);
+
+// hc_viz.cu: display variables and views over a solver's interior state,
+// AoS-6 FP64 on the device, `stride` cells between neighbours per axis
+struct VizState {
+    const double* U;       // the first interior cell
+    long long stride[3];
+    hc_solver_desc d;
+};
+int viz_display(const VizState& st, int var, int zero_border, double* out_dev, cudaStream_t s);
+int viz_range(const VizState& st, int var, double out[4], cudaStream_t s);
+int viz_render(const VizState& st, const hc_render& r, unsigned char* out_dev, cudaStream_t s);
 // initial conditions (hc_init.cu): the interior in AoS-6 FP64, x fastest, into device memory
 int init_validate(const hc_init& ic, const hc_solver_desc& d);
 int init_fill(const hc_init& ic, const hc_solver_desc& d, double* dst, cudaStream_t s);

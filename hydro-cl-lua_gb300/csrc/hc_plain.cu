@@ -334,6 +334,7 @@ struct PlainSolver {
 };
 
 long long plain_num_cells(const PlainSolver* p) { return p->p.numCells; }
+const double* plain_state_dev(const PlainSolver* p) { return reinterpret_cast<const double*>(p->U); }
 
 static int alloc(void** ptr, size_t bytes) {
     cudaError_t e = cudaMalloc(ptr, bytes);

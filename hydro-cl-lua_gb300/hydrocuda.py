@@ -99,6 +99,34 @@ class Init(ctypes.Structure):
 
 INIT_KINDS = {"sod": 0, "blast": 1, "quadrant": 2, "kelvin-helmholtz": 3}
 
+# HC_DISPLAY_*: the reference's display variable names (hydro/eqn/euler.lua:240-260,
+# the state fields of eqn.lua:913-915), vectors by component
+DISPLAY_VARS = ["rho", "m x", "m y", "m z", "m mag", "ETotal", "ePot", "v x", "v y", "v z", "v mag", "P",
+                "eInt", "eKin", "eTotal", "EInt", "EKin", "EPot", "S", "H", "h", "HTotal", "hTotal",
+                "speed of sound", "Mach number", "temperature"]
+RENDER_MODES = {"heatmap": 0, "volume": 1, "lic": 2}
+PALETTES = ["white-rainbow-black", "stripes", "blue", "paraview-red-grey-blue"]
+
+
+class Render(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("var", ctypes.c_int), ("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("palette", ctypes.c_int), ("use_log", ctypes.c_int),
+                ("value_min", ctypes.c_double), ("value_max", ctypes.c_double),
+                ("bbox", ctypes.c_double * 4), ("slice_angle", ctypes.c_double * 4), ("fixed_z", ctypes.c_double),
+                ("eye", ctypes.c_double * 3), ("fov_y", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("alpha_gamma", ctypes.c_double), ("num_isobars", ctypes.c_double),
+                ("max_iter", ctypes.c_int), ("use_isobars", ctypes.c_int), ("use_lighting", ctypes.c_int),
+                ("lic_iter", ctypes.c_int), ("noise_size", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("noise_seed", ctypes.c_ulonglong)]
+
+
+def display_index(var):
+    if isinstance(var, str):
+        if var not in DISPLAY_VARS:
+            raise ValueError("unknown display variable %r" % (var,))
+        return DISPLAY_VARS.index(var)
+    return int(var)
+
 
 # every entry point of include/hydrocuda.h with its argument types
 _vp, _dp, _ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
@@ -142,6 +170,10 @@ PROTOTYPES = {
     "hc_batch_conservation": (_ip, [_vp, _ip, _dp]),
     "hc_batch_autotune": (_ip, [_vp, ctypes.c_char_p]),
     "hc_batch_set_schedule": (_ip, [_vp, _ip, _ip]),
+    "hc_solver_display": (_ip, [_vp, _ip, _ip, _dp]),
+    "hc_solver_display_range": (_ip, [_vp, _ip, _dp]),
+    "hc_render_defaults": (_ip, [_ip, ctypes.POINTER(Render)]),
+    "hc_solver_render": (_ip, [_vp, ctypes.POINTER(Render), _vp]),
     "hc_calc_dt_noalloc": (_ip, [ctypes.POINTER(SolverDesc), _vp, _vp, _vp]),
 }
 
@@ -219,6 +251,30 @@ def _index(table, name, what):
         return table.index(name)
     except ValueError:
         raise ValueError("unknown %s %r" % (what, name))
+
+
+def make_render(mode="heatmap", **kw):
+    """hc_render with the reference's defaults for `mode`, updated from kw
+    (var may be a display variable name, palette a palette name)."""
+    L = load_library()
+    r = Render()
+    _check(L.hc_render_defaults(RENDER_MODES[mode], ctypes.byref(r)))
+    for k, v in kw.items():
+        if k == "var":
+            v = display_index(v)
+        elif k == "palette" and isinstance(v, str):
+            v = PALETTES.index(v)
+        elif k in ("use_log", "use_isobars", "use_lighting"):
+            v = int(bool(v))
+        if k in ("bbox", "slice_angle", "eye"):
+            arr = getattr(r, k)
+            for i, x in enumerate(v):
+                arr[i] = float(x)
+        elif not hasattr(r, k):
+            raise ValueError("hc_render has no field %r" % (k,))
+        else:
+            setattr(r, k, v)
+    return r
 
 
 def make_init(kind, **params):
@@ -375,6 +431,31 @@ class Solver:
         else:
             out = np.empty((5, self.num_interior), dtype=np.float32)
         _check(self.L.hc_solver_get_state(self.h, out.ctypes.data, LAYOUTS[layout], int(bool(withGhosts))))
+        return out
+
+    # display ------------------------------------------------------------------
+    def display(self, var, zeroBorder=False):
+        """calcDisplayVarToBuffer: the display variable at every cell of the grid,
+        ghosts included (shape: the grid with ghosts, z, y, x)."""
+        shape = tuple(self.gridSize[k] + 4 for k in reversed(range(self.dim)))
+        out = np.empty(shape, dtype=np.float64)
+        _check(self.L.hc_solver_display(self.h, display_index(var), int(bool(zeroBorder)),
+                                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def displayRange(self, var):
+        """calcDisplayVarRangeAndAvgAndStdDev: (min, max, mean, standard deviation)."""
+        out = (ctypes.c_double * 4)()
+        _check(self.L.hc_solver_display_range(self.h, display_index(var), out))
+        return tuple(out)
+
+    def render(self, mode="heatmap", var="rho", **kw):
+        """An RGBA8 image (height, width, 4) of the state: mode 'heatmap'
+        (2d_heatmap.glsl), 'volume' (volumetric.glsl) or 'lic'
+        (vector_lic.glsl); keyword arguments set hc_render fields."""
+        r = make_render(mode, var=var, **kw)
+        out = np.empty((r.height, r.width, 4), dtype=np.uint8)
+        _check(self.L.hc_solver_render(self.h, ctypes.byref(r), out.ctypes.data))
         return out
 
     # the reference's solver verbs -------------------------------------------

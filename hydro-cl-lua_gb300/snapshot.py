@@ -16,6 +16,8 @@ work with every precision form of the library: the state goes through the
 ghost-inclusive state I/O of the C ABI.
 """
 import os
+import struct
+import zlib
 
 import numpy as np
 
@@ -143,3 +145,48 @@ def restore(solver, path):
     if "HCTIME" in hdr:
         solver.t = float(hdr["HCTIME"])
     return hdr
+
+
+def write_png(path, rgba):
+    """Writes an RGBA8 image from the library's views (row 0 at the bottom, as
+    glReadPixels returns it) as a PNG file, top row first."""
+    img = np.ascontiguousarray(np.asarray(rgba, dtype=np.uint8)[::-1])
+    h, w, c = img.shape
+    if c != 4:
+        raise ValueError("expected an RGBA image")
+    raw = b"".join(b"\0" + img[y].tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xffffffff)
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))
+    return path
+
+
+def read_png(path):
+    """Reads a PNG written by write_png back into the library's row order."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError("not a PNG file")
+    off, idat, w, h = 8, b"", 0, 0
+    while off < len(data):
+        n, = struct.unpack(">I", data[off:off + 4])
+        tag = data[off + 4:off + 8]
+        body = data[off + 8:off + 8 + n]
+        if tag == b"IHDR":
+            w, h, depth, ctype = struct.unpack(">IIBB", body[:10])
+            if depth != 8 or ctype != 6:
+                raise ValueError("only 8-bit RGBA PNG files are read")
+        elif tag == b"IDAT":
+            idat += body
+        off += 12 + n
+    raw = zlib.decompress(idat)
+    rows = np.frombuffer(raw, dtype=np.uint8).reshape(h, 1 + 4 * w)
+    if rows[:, 0].any():
+        raise ValueError("filtered PNG rows are not read")
+    return np.ascontiguousarray(rows[:, 1:].reshape(h, w, 4)[::-1])

@@ -313,6 +313,92 @@ int hc_batch_autotune(hc_batch* b, const char* cache_path);
  * dimension `dim`.  HC_ERR_INVALID if this scheme has no such schedule. */
 int hc_batch_set_schedule(hc_batch* b, int dim, int variant);
 
+/* ---- headless visualisation ----------------------------------------------------
+ *
+ * The reference's display variables of the Euler equations
+ * (hydro/eqn/euler.lua:240-260, the state fields of eqn.lua:913-915; vector
+ * variables by component and magnitude), evaluated on the device in double
+ * with the reference's expressions. */
+#define HC_DISPLAY_RHO              0   /* U rho */
+#define HC_DISPLAY_MX               1   /* U m x */
+#define HC_DISPLAY_MY               2
+#define HC_DISPLAY_MZ               3
+#define HC_DISPLAY_M_MAG            4   /* U m mag */
+#define HC_DISPLAY_ETOTAL           5   /* U ETotal */
+#define HC_DISPLAY_EPOT             6   /* U ePot */
+#define HC_DISPLAY_VX               7   /* U v x */
+#define HC_DISPLAY_VY               8
+#define HC_DISPLAY_VZ               9
+#define HC_DISPLAY_V_MAG           10
+#define HC_DISPLAY_P               11
+#define HC_DISPLAY_EINT_SPECIFIC   12   /* eInt */
+#define HC_DISPLAY_EKIN_SPECIFIC   13   /* eKin */
+#define HC_DISPLAY_ETOTAL_SPECIFIC 14   /* eTotal */
+#define HC_DISPLAY_EINT            15   /* EInt */
+#define HC_DISPLAY_EKIN            16   /* EKin */
+#define HC_DISPLAY_EPOT_VOLUME     17   /* EPot */
+#define HC_DISPLAY_S               18
+#define HC_DISPLAY_H               19
+#define HC_DISPLAY_H_SPECIFIC      20   /* h */
+#define HC_DISPLAY_HTOTAL          21
+#define HC_DISPLAY_HTOTAL_SPECIFIC 22   /* hTotal */
+#define HC_DISPLAY_CS              23   /* speed of sound */
+#define HC_DISPLAY_MACH            24   /* Mach number */
+#define HC_DISPLAY_TEMPERATURE     25
+#define HC_NUM_DISPLAY_VARS        26
+
+/* calcDisplayVarToBuffer (solverbase.lua:1950-2065): `var` at every cell of
+ * the grid, ghosts included (numGhost = 2 on each active axis, x fastest),
+ * into `out` (host doubles).  A ghost cell shows its nearest interior cell,
+ * or 0 when zero_border is set. */
+int hc_solver_display(hc_solver* s, int var, int zero_border, double* out);
+/* calcDisplayVarRangeAndAvgAndStdDev (solverbase.lua:2871-2994): out = {min,
+ * max, mean, standard deviation}; min and max over the grid (equal to those
+ * of the interior, ghosts showing interior cells), mean and deviation over
+ * the interior cells. */
+int hc_solver_display_range(hc_solver* s, int var, double out[4]);
+
+/* Views: the shader arithmetic of hydro/draw/2d_heatmap.glsl, volumetric.glsl
+ * and vector_lic.glsl, rendered by CUDA kernels into an RGBA8 image (row 0 at
+ * the bottom, as glReadPixels returns it); no graphics API is involved. */
+#define HC_RENDER_HEATMAP  0   /* a slice of `var` through the palette */
+#define HC_RENDER_VOLUME   1   /* a ray march through a 3D grid */
+#define HC_RENDER_LIC      2   /* line-integral convolution of the velocity, coloured by |v| */
+
+/* the palettes written out in hydro/draw/palette.lua, in its order */
+#define HC_PALETTE_WHITE_RAINBOW_BLACK 0
+#define HC_PALETTE_STRIPES             1
+#define HC_PALETTE_BLUE                2
+#define HC_PALETTE_PARAVIEW            3   /* paraview-red-grey-blue */
+
+typedef struct hc_render {
+    int mode;                 /* HC_RENDER_* */
+    int var;                  /* HC_DISPLAY_* (heat map and volume) */
+    int width, height;        /* pixels */
+    int palette;              /* HC_PALETTE_* */
+    int use_log;              /* logarithmic palette mapping (draw.glsl:52-71) */
+    double value_min, value_max;   /* mapped onto the palette; min >= max: the variable's range */
+    double bbox[4];           /* heat map / LIC: chart rectangle x1, y1, x2, y2 the image covers;
+                                 all equal: the domain */
+    double slice_angle[4];    /* displaySliceAngle quaternion (x, y, z, w) */
+    double fixed_z;           /* displayFixed.y: chart z of the slice before the rotation */
+    double eye[3];            /* volume: camera position (chart coordinates), looking at the domain's centre */
+    double fov_y;             /* volume: vertical field of view, degrees */
+    double alpha, alpha_gamma, num_isobars;   /* volume: volumetric.glsl uniforms */
+    int max_iter;             /* volume: maxiter */
+    int use_isobars, use_lighting;
+    int lic_iter;             /* LIC: integralMaxIter */
+    int noise_size;           /* LIC: noise texture edge (drawVectorLICNoiseSize) */
+    int reserved;
+    unsigned long long noise_seed;   /* LIC: SplitMix64 seed of the noise texture */
+} hc_render;
+
+/* The reference's defaults for a view (palette 1, identity slice rotation,
+ * integralMaxIter 10, noise 1024^2) and a 512 x 512 image. */
+int hc_render_defaults(int mode, hc_render* out);
+/* Renders the solver's state into rgba (host, width * height * 4 bytes). */
+int hc_solver_render(hc_solver* s, const hc_render* r, unsigned char* rgba);
+
 /* ---- calcDT without allocation ---------------------------------------------
  *
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -36,7 +36,8 @@ def test_struct_layouts_match_header(tmp_path):
     import subprocess
     import hydrocuda
     structs = {"hc_solver_desc": hydrocuda.SolverDesc, "hc_batch_desc": hydrocuda.BatchDesc,
-               "hc_done": hydrocuda.Done, "hc_batch_stats": hydrocuda.BatchStats, "hc_init": hydrocuda.Init}
+               "hc_done": hydrocuda.Done, "hc_batch_stats": hydrocuda.BatchStats, "hc_init": hydrocuda.Init,
+               "hc_render": hydrocuda.Render}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "hydrocuda.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append('printf("%%s %%zu\\n", "%s", sizeof(%s));' % (cname, cname))
@@ -83,6 +84,21 @@ def test_descriptor_mapping_follows_reference_names():
     assert hydrocuda.make_desc(dict(dim=1, gridSize=8, usePLM="plm athena")).recon == 4
     with pytest.raises(ValueError):
         hydrocuda.make_desc(dict(dim=1, gridSize=8, usePLM="ppm"))
+
+
+def test_render_defaults_without_a_device():
+    """The reference's view defaults (integralMaxIter 10, 1024^2 noise, the
+    identity slice rotation, palette 1) and rejection of unknown modes."""
+    import hydrocuda
+    r = hydrocuda.make_render("lic")
+    assert (r.mode, r.lic_iter, r.noise_size, r.palette) == (2, 10, 1024, 0)
+    assert list(r.slice_angle) == [0.0, 0.0, 0.0, 1.0]
+    r = hydrocuda.make_render("heatmap", var="Mach number", palette="blue", width=64)
+    assert (r.var, r.palette, r.width) == (hydrocuda.DISPLAY_VARS.index("Mach number"), 2, 64)
+    L = hydrocuda.load_library()
+    assert L.hc_render_defaults(7, ctypes.byref(hydrocuda.Render())) == -1
+    with pytest.raises(ValueError):
+        hydrocuda.make_render("heatmap", var="vorticity")
 
 
 def test_init_defaults_without_a_device():

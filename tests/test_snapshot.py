@@ -46,3 +46,11 @@ def test_fits_round_trip_and_header(tmp_path):
     # big-endian doubles right after the header block
     first = np.frombuffer(raw, dtype=">f8", count=1, offset=2880)[0]
     assert first == full[0, 0]
+
+
+def test_png_round_trip(tmp_path):
+    img = np.random.default_rng(3).integers(0, 256, size=(5, 7, 4), dtype=np.uint8)
+    p = snapshot.write_png(str(tmp_path / "v.png"), img)
+    with open(p, "rb") as f:
+        assert f.read(8) == b"\x89PNG\r\n\x1a\n"
+    np.testing.assert_array_equal(snapshot.read_png(p), img)

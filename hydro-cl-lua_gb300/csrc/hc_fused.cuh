@@ -199,15 +199,55 @@ __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int 
     }
 }
 
+// L2 prefetch of the box tma_load<RANK> would copy with the same coordinates
+// (cp.async.bulk.prefetch.tensor: no shared memory, no completion to wait for).
+template <int RANK>
+__device__ __forceinline__ void tma_prefetch_l2(const CUtensorMap* map, int c0, int c1, int c2, int c3) {
+    uint64_t const m = reinterpret_cast<uint64_t>(map);
+    if (RANK == 2) {
+        asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(m), "r"(c0), "r"(c1)
+                     : "memory");
+    } else if (RANK == 3) {
+        asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(m), "r"(c0), "r"(c1),
+                     "r"(c2) : "memory");
+    } else {
+        asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global.tile [%0, {%1, %2, %3, %4}];" ::"l"(m), "r"(c0),
+                     "r"(c1), "r"(c2), "r"(c3) : "memory");
+    }
+}
+
 // ---------------------------------------------------------------------------
 // per-cell helpers shared by the stage kernel and the auxiliary kernels
 // ---------------------------------------------------------------------------
 
-template <int DIM>
-__device__ __forceinline__ long long padIndex(const DevInst& I, int gx, int gy, int gz) {
+template <int DIM, class GI>
+__device__ __forceinline__ long long padIndex(const GI& I, int gx, int gy, int gz) {
     long long const y = DIM > 1 ? gy + kG : 0;
     long long const z = DIM > 2 ? gz + kG : 0;
     return (z * I.py + y) * I.px + (gx + kG);
+}
+
+// The instance geometry the per-cell code indexes with, held in registers for
+// a tile: the instance itself lives in global memory, and after each store of
+// a cell the compiler would have to load its fields again (a store through a
+// T* may alias them).
+struct Geo {
+    long long plane;
+    int px, py;
+    int n[3];
+    int bc[6];
+};
+
+__device__ __forceinline__ Geo geoOf(const DevInst& I) {
+    Geo g;
+    g.plane = I.plane;
+    g.px = I.px;
+    g.py = I.py;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) g.n[k] = I.n[k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) g.bc[k] = I.bc[k];
+    return g;
 }
 
 // Per-tile constants: everything the sweeps and the cell epilogue need from
@@ -337,8 +377,8 @@ __device__ __forceinline__ T dtCell(const T* u, const TileK<T>& K, const DevInst
 // mirror reflects with the normal momentum negated, freeflow repeats the edge
 // cell.  Corner ghosts are never read by the dimension-split stencil and are
 // not written.
-template <typename T, int DIM>
-__device__ __forceinline__ void scatterGhosts(const DevInst& I, T* base, int gx, int gy, int gz, const T* u) {
+template <typename T, int DIM, class GI>
+__device__ __forceinline__ void scatterGhosts(const GI& I, T* base, int gx, int gy, int gz, const T* u) {
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         int const c = d == 0 ? gx : (d == 1 ? gy : gz), N = I.n[d];
@@ -740,6 +780,18 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             if (DIM == 1) tma_load<2>(box, map, x0, 0, 0, 0, bar);
             else if (DIM == 2) tma_load<3>(box, map, x0, y0, 0, 0, bar);
             else tma_load<4>(box, map, x0, y0, z0, 0, bar);
+            // the box of this CTA's next item into L2 while this one is computed
+            int const next = item + (int)gridDim.x;
+            if (next < nitems) {
+                int4 const nt = a.items[next];
+                const DevCtl* nc = a.ctl + nt.x;
+                if (nc->stepping) {
+                    const CUtensorMap* nmap = a.tmaps + (size_t)nt.x * kMaxBufs + slotBuf(st.in_buf, nc->rot, a.rot_buf);
+                    if (DIM == 1) tma_prefetch_l2<2>(nmap, nt.y * TX, 0, 0, 0);
+                    else if (DIM == 2) tma_prefetch_l2<3>(nmap, nt.y * TX, nt.z * TY, 0, 0);
+                    else tma_prefetch_l2<4>(nmap, nt.y * TX, nt.z * TY, nt.w * TZ, 0);
+                }
+            }
         }
         // the tile's constants (loads; no FP64 arithmetic) while the tile streams in
         TileK<T> K;
@@ -826,6 +878,44 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
         bool const useCur = K.useCur;
         T* out = reinterpret_cast<T*>(I.buf[slotBuf(st.out_buf, rot, a.rot_buf)]);
         T* dstore = st.store_deriv >= 0 ? reinterpret_cast<T*>(I.dbuf[st.store_deriv]) : nullptr;
+        // The geometry and source buffers the cells of a segment use.  With
+        // registers to spare (the launch bounds leave >= 96 a thread) they are
+        // loaded into registers once per segment, after its sweep; otherwise
+        // the cell code reads them from the instance (holding them would make
+        // the register-tight schedules spill).
+        constexpr bool HOIST = 65536 / (NT * (OCC > 0 ? OCC : 1)) >= 96;
+        Geo geo;
+        const T* asrc[4];
+        bool afromBox[4];
+        const T* bsrc[4];
+        auto loadEpilogue = [&]() {
+            if constexpr (HOIST) {
+                geo = geoOf(I);
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    int const b = m < st.n_alpha ? slotBuf(st.alpha_buf[m], rot, a.rot_buf) : inBuf;
+                    afromBox[m] = b == inBuf;
+                    asrc[m] = reinterpret_cast<const T*>(I.buf[b]);
+                    bsrc[m] = m < st.n_beta ? reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]) : nullptr;
+                }
+            }
+        };
+        auto const& gi = [&]() -> decltype(auto) {
+            if constexpr (HOIST) return (geo);
+            else return (I);
+        }();
+        auto fromBoxA = [&](int m) -> bool {
+            if constexpr (HOIST) return afromBox[m];
+            else return slotBuf(st.alpha_buf[m], rot, a.rot_buf) == inBuf;
+        };
+        auto srcA = [&](int m) -> const T* {
+            if constexpr (HOIST) return asrc[m];
+            else return reinterpret_cast<const T*>(I.buf[slotBuf(st.alpha_buf[m], rot, a.rot_buf)]);
+        };
+        auto srcB = [&](int m) -> const T* {
+            if constexpr (HOIST) return bsrc[m];
+            else return reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
+        };
         T const arF = K.area[AX];
         bool const skipF = K.skip[AX];
         T dtmin = fast::M<T>::inf();
@@ -835,7 +925,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
         // Runge-Kutta combination, constrainU, store, ghost copies, stored
         // derivative, CFL dt
         auto finishCell = [&](int gx, int gy, int gz, int bi, const T* Dc) {
-            long long const idx = padIndex<DIM>(I, gx, gy, gz);
+            long long const idx = padIndex<DIM>(gi, gx, gy, gz);
             T u[5], deriv[5];
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
@@ -847,22 +937,21 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 if (m >= st.n_alpha) break;
-                int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
-                if (b == inBuf) {
+                if (fromBoxA(m)) {
 #pragma unroll
                     for (int f = 0; f < 5; ++f) u[f] = u[f] + box[f * G::BOXN + bi] * K.calpha[m];
                 } else {
-                    const T* src = reinterpret_cast<const T*>(I.buf[b]);
+                    const T* src = srcA(m);
 #pragma unroll
-                    for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * K.calpha[m];
+                    for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * gi.plane + idx] * K.calpha[m];
                 }
             }
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 if (m >= st.n_beta) break;
-                const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
+                const T* src = srcB(m);
 #pragma unroll
-                for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * I.plane + idx] * K.cbeta[m];
+                for (int f = 0; f < 5; ++f) u[f] = u[f] + src[f * gi.plane + idx] * K.cbeta[m];
             }
             if (useCur) {
 #pragma unroll
@@ -870,13 +959,13 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             }
             constrainCell<T, EXACT>(u, K);
 #pragma unroll
-            for (int f = 0; f < 5; ++f) out[f * I.plane + idx] = u[f];
+            for (int f = 0; f < 5; ++f) out[f * gi.plane + idx] = u[f];
             // after constrainU a non-finite momentum shows in ETotal
             bad |= !fast::M<T>::finite_(u[0] + u[4]);
-            scatterGhosts<T, DIM>(I, out, gx, gy, gz, u);
+            scatterGhosts<T, DIM>(gi, out, gx, gy, gz, u);
             if (dstore) {
 #pragma unroll
-                for (int f = 0; f < 5; ++f) dstore[f * I.plane + idx] = deriv[f];
+                for (int f = 0; f < 5; ++f) dstore[f * gi.plane + idx] = deriv[f];
             }
             if (st.last) dtmin = fast::tmin(dtmin, dtCell<T, EXACT, DIM>(u, K, I));
         };
@@ -889,7 +978,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
         auto finishFast = [&](auto vtag, int gx, int gy, int gz, int bi, const T* Dc, bool second) {
             using V = decltype(vtag);
             constexpr int NL = lanes::nlanes<V>();
-            long long const idx = padIndex<DIM>(I, gx, gy, gz);
+            long long const idx = padIndex<DIM>(gi, gx, gy, gz);
             auto ld = [&](const T* p) -> V {
                 if constexpr (NL == 1) return *p;
                 else return *reinterpret_cast<const float2*>(p);
@@ -913,14 +1002,13 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             // of the alphas (summed directly, RK3-TVD's 1/3 and 2/3 rounded to
             // FP32 add 3e-8 of every conserved quantity per step)
             auto ldAlpha = [&](int m, V* v) {
-                int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
-                if (b == inBuf) {
+                if (fromBoxA(m)) {
 #pragma unroll
                     for (int f = 0; f < 5; ++f) v[f] = ld(box + f * G::BOXN + bi);
                 } else {
-                    const T* src = reinterpret_cast<const T*>(I.buf[b]);
+                    const T* src = srcA(m);
 #pragma unroll
-                    for (int f = 0; f < 5; ++f) v[f] = ld(src + f * I.plane + idx);
+                    for (int f = 0; f < 5; ++f) v[f] = ld(src + f * gi.plane + idx);
                 }
             };
             int const last = st.n_alpha - 1;
@@ -942,10 +1030,10 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 if (m >= st.n_beta) break;
-                const T* src = reinterpret_cast<const T*>(I.dbuf[st.beta_buf[m]]);
+                const T* src = srcB(m);
                 V const c = lanes::splat<V>(K.cbeta[m]);
 #pragma unroll
-                for (int f = 0; f < 5; ++f) u[f] = lanes::fma(ld(src + f * I.plane + idx), c, u[f]);
+                for (int f = 0; f < 5; ++f) u[f] = lanes::fma(ld(src + f * gi.plane + idx), c, u[f]);
             }
             if (useCur) {
                 V const c = lanes::splat<V>(cbcur);
@@ -954,10 +1042,10 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             }
             lanes::constrain<V>(u, le, K.invg1);
 #pragma unroll
-            for (int f = 0; f < 5; ++f) st_(out + f * I.plane + idx, u[f]);
+            for (int f = 0; f < 5; ++f) st_(out + f * gi.plane + idx, u[f]);
             if (dstore) {
 #pragma unroll
-                for (int f = 0; f < 5; ++f) st_(dstore + f * I.plane + idx, deriv[f]);
+                for (int f = 0; f < 5; ++f) st_(dstore + f * gi.plane + idx, deriv[f]);
             }
             V dtv;
             if (st.last) dtv = lanes::dtCell<V, DIM>(u, le, K.gdx);
@@ -969,7 +1057,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
                 for (int f = 0; f < 5; ++f) uu[f] = lanes::lane(u[f], l);
                 // after constrainU a non-finite momentum shows in ETotal
                 bad |= !fast::M<T>::finite_(uu[0] + uu[4]);
-                scatterGhosts<T, DIM>(I, out, gx + l, gy, gz, uu);
+                scatterGhosts<T, DIM>(gi, out, gx + l, gy, gz, uu);
                 if (st.last) dtmin = fast::tmin(dtmin, lanes::lane(dtv, l));
             }
         };
@@ -1000,6 +1088,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             int const gA0 = AX == 0 ? gx0 : (AX == 1 ? gy0 : gz0);
             int const nA = AX == 0 ? nx : (AX == 1 ? ny : nz);
             int const kmax = nA - gA0 < L ? nA - gA0 : L;
+            loadEpilogue();
             if constexpr (EXACT) {
 #pragma unroll 1
                 for (int k = 0; k < kmax; ++k) {

@@ -75,21 +75,6 @@ __global__ void k_set_dt(DevCtl* ctl, const DevInst* inst, int slot, double dt, 
     }
 }
 
-// For timing a stage in isolation: mark live slots as stepping with their
-// current CFL dt, without touching t, steps or the dt parity.
-__global__ void k_tune_mode(DevCtl* ctl, const DevInst* inst, int nslots, int on, BetaTable bt) {
-    int const s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nslots) return;
-    DevCtl& c = ctl[s];
-    if (!on) { c.stepping = 0; return; }
-    if (!c.active) return;
-    const DevInst& I = inst[s];
-    double const dt = I.fixed_dt > 0 ? I.fixed_dt : I.cfl * __longlong_as_double((long long)c.dtmin[c.par]);
-    c.dt = isfinite(dt) && dt > 0 ? dt : 0.;
-    fillStepCoefs(c, I, bt, c.dt);
-    c.stepping = 1;
-}
-
 __global__ void k_reset_dtmin(DevCtl* ctl, int slot) {
     ctl[slot].dtmin[ctl[slot].par] = kInfBits;
 }
@@ -919,33 +904,29 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
             reencode_all(f, dim);
             f->items_dirty = true;
             HC_CHECK(rebuild_items(f));
+            // whole steps of the live batch (every schedule gives the same
+            // bits, so this is plain stepping): one warm-up, `reps` timed
+            int const mask = f->graph_dims_mask;
             unsigned const g = (unsigned)((f->max_slots + 127) / 128);
-            fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->betas);
-            StagePlan sp = f->plan[0].stage[0];
-            sp.last = 0;   // no dt atomics while timing
-            IntegratorPlan one;
-            std::memset(&one, 0, sizeof(one));
-            one.n_stages = 1;
-            one.stage[0] = sp;
-            HC_CHECK(launch_stages(f, one, 1 << (dim - 1)));   // warm-up
+            HC_CHECK(launch_step(f, mask));
             cudaEvent_t e0, e1;
-            cudaEventCreate(&e0);
-            cudaEventCreate(&e1);
+            HC_CUDA(cudaEventCreate(&e0));
+            HC_CUDA(cudaEventCreate(&e1));
             cudaEventRecord(e0, f->stream);
-            int const reps = 5;
-            for (int r = 0; r < reps; ++r) HC_CHECK(launch_stages(f, one, 1 << (dim - 1)));
+            int const reps = 3;
+            for (int r = 0; r < reps; ++r) HC_CHECK(launch_step(f, mask));
             cudaEventRecord(e1, f->stream);
+            fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas);
             cudaEventSynchronize(e1);
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
-            fz::k_tune_mode<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->betas);
             HC_CUDA(cudaStreamSynchronize(f->stream));
             const StageLauncher* Lc = f->launcher[dim - 1];
             log << "# " << key << " variant " << v << " tile " << Lc->tx << "x" << Lc->ty << "x" << Lc->tz << " threads "
                 << Lc->nthreads << " seg " << Lc->seg << " unroll " << Lc->unroll << " ctas/SM " << Lc->min_ctas
-                << " lanes " << Lc->lanes << " slope " << Lc->slope << " ms/stage " << ms / reps << "\n";
+                << " lanes " << Lc->lanes << " slope " << Lc->slope << " ms/step " << ms / reps << "\n";
             if (ms < bestMs) { bestMs = ms; best = v; }
         }
         f->tune_log += log.str();

@@ -1,10 +1,12 @@
 /*
  * hydrocuda.h -- C ABI of libhydrocuda.so, a GB300 (sm_103a) implementation of
- * hydro-cl-lua's finite-volume Euler update: ghost-cell boundary fill, "plm
- * cons" reconstruction with the reference's slope limiters, the Roe flux on
- * the Euler eigen-decomposition (optionally flux-limited), calcDerivFromFlux,
- * the CFL calcDT min-reduction, constrainU, and the explicit forward-Euler and
- * Runge-Kutta integrators.
+ * hydro-cl-lua's finite-volume Euler update: ghost-cell boundary fill, PLM
+ * reconstruction ("plm cons", "plm prim", "plm athena") with the reference's
+ * slope limiters, the Roe flux on the Euler eigen-decomposition (optionally
+ * flux-limited) or the HLL / Rusanov / HLLC fluxes, calcDerivFromFlux, the CFL
+ * calcDT min-reduction, constrainU, and the explicit forward-Euler and
+ * Runge-Kutta integrators; batched solving and serving; initial conditions
+ * built on the device; display variables and headless views.
  *
  * Plain C99; no callbacks; no library types in the signatures.  Every entry
  * point returns 0 (HC_OK) or a negative HC_ERR_* code; hc_last_error() gives a
@@ -25,6 +27,8 @@
  *   update                hydro/solver/solverbase.lua:3026-3190
  *   App exit loop         hydro/app.lua:1573-1600 (t >= exitTime checked before stepping)
  *   UBuf readback         hydro/solver/gridsolver.lua:1337-1366 (UBufObj:toCPU)
+ *   display variables     hydro/solver/solverbase.lua:1950-2065, 2871-2994
+ *   views                 hydro/draw/2d_heatmap.glsl, volumetric.glsl, vector_lic.glsl
  */
 #ifndef HYDROCUDA_H
 #define HYDROCUDA_H
@@ -305,8 +309,11 @@ int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout);
 int hc_batch_retire(hc_batch* b, int slot);
 int hc_batch_stats_get(hc_batch* b, hc_batch_stats* out);
 int hc_batch_conservation(hc_batch* b, int slot, double sums[5]);
-/* Times the candidate tile shapes on the batch's current work list and keeps
- * the fastest; reads/writes the choice from/to cache_path when not NULL. */
+/* Times the candidate schedules (tile shape, segment length, threads) of the
+ * stage kernel on the batch's live instances and keeps the fastest; reads /
+ * writes the choice from / to cache_path when not NULL.  Timing runs whole
+ * steps (4 per candidate): the live solves advance by those steps, exactly as
+ * hc_batch_step would advance them (every schedule gives the same bits). */
 int hc_batch_autotune(hc_batch* b, const char* cache_path);
 /* Pins the schedule (tile shape, segment length, threads, lanes: the
  * `variant` numbers of the autotuner's log) of the stage kernel for grids of

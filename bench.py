@@ -474,12 +474,28 @@ def batch_solve(hc, ctx, args, cons, precision, t_end=math.inf, max_steps=0, chu
     Returns the final AoS-6 interior state, updates done, device ms and the
     Kahan FP64 sums of the conserved fields before and after; with
     `checkpoints` (update counts) also the state after each of them."""
+    tune = None
+    if precision == "f32":
+        # the schedule is tuned on a throwaway batch of the same grid (tuning
+        # advances the solve it times), then read from the cache
+        tune = os.path.join(PKG, "_build", "autotune_single.txt")
+        tb = hc.Batch(ctx, precision=precision, max_slots=1, **_scheme(args))
+        try:
+            if init is not None:
+                tb.admit_init(args, init[0], t_end=math.inf, tag=0, **init[1])
+            else:
+                tb.admit(args, cons, t_end=math.inf, tag=0)
+            tb.autotune(tune)
+        finally:
+            tb.close()
     b = hc.Batch(ctx, precision=precision, max_slots=1, **_scheme(args))
     try:
         if init is not None:
             slot = b.admit_init(args, init[0], t_end=t_end, max_steps=max_steps, tag=0, **init[1])
         else:
             slot = b.admit(args, cons, t_end=t_end, max_steps=max_steps, tag=0)
+        if tune:
+            b.autotune(tune)
         sums0 = b.conservation(slot)
         total_ms = 0.0
         ev = []

@@ -83,8 +83,12 @@ int validate_desc(const hc_solver_desc* d) {
         if (!(d->maxs[k] > d->mins[k])) return fail(HC_ERR_INVALID, "maxs must exceed mins");
     }
     for (int k = 0; k < 6; ++k)
-        if (d->boundary[k] < HC_BOUNDARY_NONE || d->boundary[k] > HC_BOUNDARY_FREEFLOW)
+        if (d->boundary[k] < HC_BOUNDARY_NONE || d->boundary[k] >= HC_NUM_BOUNDARIES)
             return fail(HC_ERR_INVALID, "unknown boundary");
+    for (int k = 0; k < d->dim; ++k)
+        for (int m = 0; m < 2; ++m)
+            if (d->boundary[2 * k + m] == HC_BOUNDARY_QUADRATIC && d->n[k] < 3)
+                return fail(HC_ERR_INVALID, "the quadratic boundary extrapolates from 3 interior cells");
     if (d->flux_limiter < 0 || d->flux_limiter >= HC_NUM_LIMITERS) return fail(HC_ERR_INVALID, "unknown flux limiter");
     if (d->slope_limiter < 0 || d->slope_limiter >= HC_NUM_LIMITERS) return fail(HC_ERR_INVALID, "unknown slope limiter");
     if (d->recon < HC_RECON_NONE || d->recon >= HC_NUM_RECONS) return fail(HC_ERR_INVALID, "unknown usePLM");

@@ -1161,6 +1161,71 @@ __global__ void k_fill_ghosts(const DevInst* inst, int slot, int buf) {
     }
 }
 
+// The linear / quadratic boundaries (gridsolver.lua:783-858) of one
+// instance's buffer: each ghost from the two (three) cells inside it, filled
+// outward (j = 0 then 1, the min side before the max side as the reference's
+// boundary kernel does), on the lines through the interior (corner ghosts are
+// never read by the dimension-split stencil).  Lines are spread over `nthr`
+// threads starting at `tid`.
+template <typename T, int DIM>
+__device__ void extrapGhosts(const DevInst& I, T* base, long long tid, long long nthr) {
+#pragma unroll 1
+    for (int d = 0; d < DIM; ++d) {
+        int const lo = I.bc[2 * d], hi = I.bc[2 * d + 1];
+        bool const xlo = lo == HC_BOUNDARY_LINEAR || lo == HC_BOUNDARY_QUADRATIC;
+        bool const xhi = hi == HC_BOUNDARY_LINEAR || hi == HC_BOUNDARY_QUADRATIC;
+        if (!xlo && !xhi) continue;
+        int const o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+        int const n1 = o1 < DIM ? I.n[o1] : 1, n2 = o2 < DIM ? I.n[o2] : 1, N = I.n[d];
+        for (long long line = tid; line < (long long)n1 * n2; line += nthr) {
+            int c[3];
+            c[o1] = (int)(line % n1);
+            c[o2] = (int)(line / n1);
+            auto at = [&](int x) -> long long {
+                c[d] = x;
+                return padIndex<DIM>(I, c[0], c[1], c[2]);
+            };
+            for (int j = 0; j < kG; ++j) {
+                for (int mm = 0; mm < 2; ++mm) {
+                    int const method = mm == 0 ? lo : hi;
+                    if (method != HC_BOUNDARY_LINEAR && method != HC_BOUNDARY_QUADRATIC) continue;
+                    int const s = mm == 0 ? -1 : 1;           // outward
+                    int const g = mm == 0 ? -1 - j : N + j;    // the ghost
+                    long long const id = at(g), i1 = at(g - s), i2 = at(g - 2 * s), i3 = at(g - 3 * s);
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) {
+                        T const a1 = base[f * I.plane + i1], a2 = base[f * I.plane + i2];
+                        base[f * I.plane + id] = method == HC_BOUNDARY_LINEAR
+                                                     ? T(2) * a1 - a2
+                                                     : T(3) * a1 - T(3) * a2 + base[f * I.plane + i3];
+                    }
+                }
+            }
+        }
+    }
+}
+
+// extrapGhosts of one instance (admission, resetState, boundary()).
+template <typename T, int DIM>
+__global__ void k_extrap_slot(const DevInst* inst, int slot, int buf) {
+    const DevInst& I = inst[slot];
+    extrapGhosts<T, DIM>(I, reinterpret_cast<T*>(I.buf[buf]), blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                         (long long)gridDim.x * blockDim.x);
+}
+
+// extrapGhosts of the output of a stage on every stepping instance of this
+// dimension (grid.y = slots); state buffer `outBuf` of the plan, rotated per slot.
+template <typename T, int DIM>
+__global__ void k_extrap_stage(const DevInst* inst, const DevCtl* ctl, int nslots, int outBuf, int rotBuf) {
+    for (int slot = blockIdx.y; slot < nslots; slot += gridDim.y) {
+        const DevInst& I = inst[slot];
+        if (I.dim != DIM || !ctl[slot].stepping) continue;
+        int const b = slotBuf(outBuf, ctl[slot].rot, rotBuf);
+        extrapGhosts<T, DIM>(I, reinterpret_cast<T*>(I.buf[b]), blockIdx.x * (long long)blockDim.x + threadIdx.x,
+                             (long long)gridDim.x * blockDim.x);
+    }
+}
+
 template <typename T, int DIM, bool EXACT>
 __global__ void k_constrain(const DevInst* inst, int slot, int buf) {
     const DevInst& I = inst[slot];
@@ -1287,6 +1352,8 @@ struct AuxLauncher {
     void (*calc_dt)(const DevInst* inst, DevCtl* ctl, int slot, int buf, cudaStream_t s);
     void (*xfer)(const DevInst* inst, int slot, int buf, void* staging, int layout, int dir, cudaStream_t s);
     void (*sums)(const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s);
+    // linear / quadratic ghosts of a stage's output on every stepping instance of this dimension
+    void (*extrap_stage)(const DevInst* inst, const DevCtl* ctl, int nslots, int out_buf, int rot_buf, cudaStream_t s);
 };
 
 void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& aux);

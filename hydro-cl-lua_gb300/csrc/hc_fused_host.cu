@@ -169,6 +169,7 @@ struct FusedSet {
     // graph of one (or two, when the state rotates) steps
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
+    int extrap_dims = 0;           // dims (bit d-1) whose live instances have a linear / quadratic boundary
     int graph_dims_mask = 0;
     std::string tune_log;          // per-variant timings of the last autotune
     DevicePool pool;               // instance state buffers
@@ -315,8 +316,8 @@ static int validate(const FusedSet* f, const hc_solver_desc& d) {
         if (!(d.maxs[k] > d.mins[k])) return fail(HC_ERR_INVALID, "maxs must exceed mins");
     }
     for (int k = 0; k < 2 * d.dim; ++k)
-        if (d.boundary[k] != HC_BOUNDARY_PERIODIC && d.boundary[k] != HC_BOUNDARY_MIRROR && d.boundary[k] != HC_BOUNDARY_FREEFLOW)
-            return fail(HC_ERR_INVALID, "the fused form supports periodic, mirror and freeflow boundaries");
+        if (d.boundary[k] == HC_BOUNDARY_NONE || d.boundary[k] < 0 || d.boundary[k] >= HC_NUM_BOUNDARIES)
+            return fail(HC_ERR_INVALID, "the fused form supports periodic, mirror, freeflow, linear and quadratic boundaries");
     for (int k = 0; k < d.dim; ++k)
         if ((d.boundary[2 * k] == HC_BOUNDARY_PERIODIC) != (d.boundary[2 * k + 1] == HC_BOUNDARY_PERIODIC))
             return fail(HC_ERR_INVALID, "periodic boundaries must be periodic on both sides of an axis");
@@ -558,9 +559,12 @@ static int rebuild_items(FusedSet* f) {
     HC_CUDA(cudaStreamSynchronize(f->stream));
     HC_CUDA(cudaMemcpy(f->h_ctl, f->d_ctl, sizeof(DevCtl) * f->max_slots, cudaMemcpyDeviceToHost));
     std::vector<int4> items[3];
+    int extrap = 0;
     for (int s = 0; s < f->max_slots; ++s) {
         const Slot& S = f->slots[s];
         if (!S.used || !f->h_ctl[s].active) continue;
+        for (int k = 0; k < 2 * S.dim; ++k)
+            if (S.inst.bc[k] == HC_BOUNDARY_LINEAR || S.inst.bc[k] == HC_BOUNDARY_QUADRATIC) extrap |= 1 << (S.dim - 1);
         const StageLauncher* L = f->launcher[S.dim - 1];
         int const ntx = (S.inst.n[0] + L->tx - 1) / L->tx;
         int const nty = S.dim > 1 ? (S.inst.n[1] + L->ty - 1) / L->ty : 1;
@@ -586,8 +590,9 @@ static int rebuild_items(FusedSet* f) {
     }
     HC_CUDA(cudaMemcpyAsync(f->d_nitems, f->h_nitems, sizeof(int) * 3, cudaMemcpyHostToDevice, f->stream));
     HC_CUDA(cudaStreamSynchronize(f->stream));
-    if (mask != f->graph_dims_mask) f->graph_valid = false;
+    if (mask != f->graph_dims_mask || extrap != f->extrap_dims) f->graph_valid = false;
     f->graph_dims_mask = mask;
+    f->extrap_dims = extrap;
     f->items_dirty = false;
     return HC_OK;
 }
@@ -630,6 +635,11 @@ static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
             fill_stage(a.st, P.stage[s], P.stage[s].index);
             f->launcher[d]->launch(a, f->sch.slope_limiter, f->sch.flux_limiter, f->grid[d], f->stream);
         }
+        // linear / quadratic ghosts of this stage's output, before the next stage reads them
+        for (int d = 0; d < 3; ++d)
+            if ((dims_mask & f->extrap_dims) & (1 << d))
+                find_aux(f->sch.precision, d + 1)->extrap_stage(f->d_inst, f->d_ctl, f->max_slots, P.stage[s].out_buf,
+                                                                f->rot_buf, f->stream);
     }
     HC_CUDA(cudaGetLastError());
     return HC_OK;

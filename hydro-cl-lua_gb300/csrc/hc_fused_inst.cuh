@@ -83,6 +83,11 @@ void add_aux(std::vector<AuxLauncher>& v) {
     a.dim = DIM;
     a.fill_ghosts = [](const DevInst* inst, int slot, int buf, cudaStream_t s) {
         k_fill_ghosts<T, DIM><<<1024, 256, 0, s>>>(inst, slot, buf);
+        k_extrap_slot<T, DIM><<<64, 256, 0, s>>>(inst, slot, buf);
+    };
+    a.extrap_stage = [](const DevInst* inst, const DevCtl* ctl, int nslots, int out_buf, int rot_buf, cudaStream_t s) {
+        unsigned const gy = (unsigned)(nslots < 65535 ? nslots : 65535);
+        k_extrap_stage<T, DIM><<<dim3(8, gy), 256, 0, s>>>(inst, ctl, nslots, out_buf, rot_buf);
     };
     a.constrain = [](const DevInst* inst, int slot, int buf, cudaStream_t s) {
         k_constrain<T, DIM, EXACT><<<1024, 256, 0, s>>>(inst, slot, buf);

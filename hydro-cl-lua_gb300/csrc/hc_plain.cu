@@ -88,6 +88,17 @@ __global__ void k_boundary(PlainParams s, Cons* U, int side) {
             } else if (method == HC_BOUNDARY_FREEFLOW) {
                 if (mm == 0) { dst = j; src = kGhost; }
                 else { dst = gsSide - kGhost + j; src = gsSide - kGhost - 1; }
+            } else if (method == HC_BOUNDARY_LINEAR || method == HC_BOUNDARY_QUADRATIC) {
+                // gridsolver.lua:783-858: outward, each ghost from the two
+                // (three) cells inside it, all 6 reals
+                int d, i1, i2, i3;
+                if (mm == 0) { d = kGhost - j - 1; i1 = kGhost - j; i2 = kGhost - j + 1; i3 = kGhost - j + 2; }
+                else { d = gsSide - kGhost + j; i1 = gsSide - kGhost + j - 1; i2 = gsSide - kGhost + j - 2; i3 = gsSide - kGhost + j - 3; }
+                Cons const a1 = at(i1), a2 = at(i2), a3 = at(i3);
+                Cons& o = at(d);
+                for (int k = 0; k < 6; ++k)
+                    o.p[k] = method == HC_BOUNDARY_LINEAR ? 2. * a1.p[k] - a2.p[k] : 3. * a1.p[k] - 3. * a2.p[k] + a3.p[k];
+                continue;
             } else {
                 continue;
             }

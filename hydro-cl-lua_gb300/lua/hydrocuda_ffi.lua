@@ -72,7 +72,7 @@ for i, name in ipairs{
 	'Runge-Kutta 3, TVD', 'Runge-Kutta 4, TVD', 'Runge-Kutta 4, non-TVD',
 } do M.integratorIndex[name] = i - 1 end
 
-M.boundaryIndex = {none = 0, periodic = 1, mirror = 2, freeflow = 3}
+M.boundaryIndex = {none = 0, periodic = 1, mirror = 2, freeflow = 3, linear = 4, quadratic = 5}
 M.fluxIndex = {roe = 0, hll = 1, rusanov = 2, ['euler-hllc'] = 3}
 M.reconIndex = {['piecewise constant'] = 1, ['plm cons'] = 2, ['plm prim'] = 3, ['plm athena'] = 4}
 M.precisionIndex = {['f64 plain'] = 0, f64 = 1, f32 = 2}

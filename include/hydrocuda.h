@@ -54,11 +54,16 @@ extern "C" {
 #define HC_ERR_TIMEOUT     -7   /* a bounded device wait ran out */
 #define HC_ERR_STATE       -8   /* call not valid in the handle's current state */
 
-/* boundary names (gridsolver.lua:617-780) */
+/* boundary names (gridsolver.lua:617-860); "fixed" needs the initial
+ * condition's generated fixedCode and the sphere / cylinder ones curvilinear
+ * coordinates: not provided */
 #define HC_BOUNDARY_NONE      0
 #define HC_BOUNDARY_PERIODIC  1
 #define HC_BOUNDARY_MIRROR    2
 #define HC_BOUNDARY_FREEFLOW  3
+#define HC_BOUNDARY_LINEAR    4   /* ghost = 2 U[i1] - U[i2], ghosts filled outward (gridsolver.lua:783-813) */
+#define HC_BOUNDARY_QUADRATIC 5   /* ghost = 3 U[i1] - 3 U[i2] + U[i3] (gridsolver.lua:815-858) */
+#define HC_NUM_BOUNDARIES     6
 
 /* limiter table, in the order of hydro/app.lua:614-635 (reference index - 1);
  * HC_LIMITER_DONOR_CELL as flux limiter means "no flux limiter" */

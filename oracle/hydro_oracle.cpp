@@ -47,7 +47,7 @@ struct prim_t { real rho; real v[3]; real P; real ePot; };
 // hydro/eqn/euler.lua:298-307 -- eigen_t
 struct eigen_t { real rho; real v[3]; real hTotal; real Cs; real vSq; real vL[3]; };
 
-enum { BC_NONE = 0, BC_PERIODIC = 1, BC_MIRROR = 2, BC_FREEFLOW = 3 };
+enum { BC_NONE = 0, BC_PERIODIC = 1, BC_MIRROR = 2, BC_FREEFLOW = 3, BC_LINEAR = 4, BC_QUADRATIC = 5 };
 enum { RECON_NONE = 0, RECON_PIECEWISE_CONSTANT = 1, RECON_PLM_CONS = 2, RECON_PLM_PRIM = 3, RECON_PLM_ATHENA = 4 };
 enum { FLUX_ROE = 0, FLUX_HLL = 1, FLUX_RUSANOV = 2, FLUX_HLLC = 3 };
 
@@ -593,6 +593,17 @@ static void boundary(Solver& s) {
 					} else if (method == BC_FREEFLOW) {
 						if (mm == 0) { dst = j; src = G; }
 						else { dst = gsSide - G + j; src = gsSide - G - 1; }
+					} else if (method == BC_LINEAR || method == BC_QUADRATIC) {
+						// gridsolver.lua:783-858: outward from the interior, each
+						// ghost from the two (three) cells inside it, all 6 reals
+						int d, i1, i2, i3;
+						if (mm == 0) { d = G - j - 1; i1 = G - j; i2 = G - j + 1; i3 = G - j + 2; }
+						else { d = gsSide - G + j; i1 = gsSide - G + j - 1; i2 = gsSide - G + j - 2; i3 = gsSide - G + j - 3; }
+						for (int k = 0; k < 6; ++k) {
+							if (method == BC_LINEAR) at(d).ptr[k] = 2. * at(i1).ptr[k] - at(i2).ptr[k];
+							else at(d).ptr[k] = 3. * at(i1).ptr[k] - 3. * at(i2).ptr[k] + at(i3).ptr[k];
+						}
+						continue;
 					} else {
 						continue;
 					}

@@ -40,7 +40,7 @@ INTEGRATORS = [
     "Runge-Kutta 2, non-TVD", "Runge-Kutta 3, TVD", "Runge-Kutta 4, TVD",
     "Runge-Kutta 4, non-TVD",
 ]
-BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3}
+BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3, "linear": 4, "quadratic": 5}
 RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2, "plm prim": 3, "plm athena": 4}
 
 

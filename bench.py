@@ -738,6 +738,17 @@ def run_c5(args):
     serve.Server(wb, steps_per_tick=4, keep_results=False).run(warm_reqs)
     wb.close()
 
+    # schedules: tuned once on a calibration batch of requests drawn from the
+    # same distribution (another seed), then pinned on the serving batch
+    # (which starts empty, so it has nothing to tune on)
+    cal = serve.synthetic_stream(48, rate_hz=1e6, seed=13, device_init=True)
+    cb = hc.Batch(ctx, precision="f32", max_slots=64, hbm_budget=budget, **scheme)
+    for r in cal:
+        cb.admit_init(r.args, r.init[0], t_end=math.inf, tag=r.tag, **r.init[1])
+    cb.autotune()
+    schedules = {d: cb.stats()["schedule"][d - 1] for d in (1, 2, 3)}
+    cb.close()
+
     device_init = not args.host_states
     reqs = serve.synthetic_stream(args.requests, rate_hz=200.0, seed=5, lazy=True, layout="soa5_f32",
                                   device_init=device_init)
@@ -755,6 +766,8 @@ def run_c5(args):
     sample_in = {r.tag: (r.args, r.init, r.t_end) for r in f64_stream if r.tag in set(sample)}
     pre = StatePrefetch(reqs) if not device_init else None
     b = hc.Batch(ctx, precision="f32", max_slots=1024, hbm_budget=budget, **scheme)
+    for d, v in schedules.items():
+        b.set_schedule(d, v)
     srv = serve.Server(b, steps_per_tick=8, keep_results=set(sample))
     t0 = time.perf_counter()
     done = srv.run(reqs)
@@ -804,6 +817,8 @@ def run_c5(args):
             "initial_states": "built on the device at admission (hc_batch_admit_init)" if device_init else
                               "built on the host by worker threads, uploaded at admission",
             "host_state_wait_s": pre.wait_s if pre else 0.0,
+            "schedules": {"by_dim": {str(d): v for d, v in schedules.items()},
+                          "note": "autotuned on a 48-request calibration batch (seed 13), then pinned"},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "peak_kind": peak_kind, "traffic": None,
                          "note": "algorithmic bytes: RK2, 5 state arrays x 5 fields x 4 B per cell-update"},

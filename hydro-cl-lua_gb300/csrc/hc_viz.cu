@@ -14,6 +14,7 @@
 //   heat map             hydro/draw/2d_heatmap.glsl:28-59
 //   volume ray march     hydro/draw/volumetric.glsl:45-110
 //   LIC                  hydro/draw/vector_lic.glsl:36-107, vector_lic.lua
+//   slice stack          hydro/draw/3d_slice.glsl:56-118, 3d_slice.lua:165-235
 //
 // The display values are computed in double with the reference's
 // expressions (this file is compiled without FMA contraction).  The image
@@ -270,6 +271,8 @@ struct View {
     int maxIter, useIsobars, useLighting;
     // LIC
     int licIter, noiseSize;
+    // slice stack
+    int sliceAxis, numSlices;
 };
 
 __device__ __forceinline__ float3 quatRotate(const float* q, float3 v) {
@@ -450,6 +453,71 @@ __global__ void k_volume(View V, Tex tex, Tex grad, uchar4* out) {
     out[(long long)py * V.width + px] = o;
 }
 
+// The volume as 3d_slice.lua draws it: num_slices + 1 quads across the grid
+// along the view axis (the one the camera looks most along), blended back to
+// front with (SRC_ALPHA, ONE_MINUS_SRC_ALPHA) onto a clear (0, 0, 0, 0)
+// framebuffer; here an orthographic view along the axis, the image spanning
+// the other two (in x, y, z order).  Each slice's fragment is 3d_slice.glsl's
+// (voxel through the palette; alpha pow(alpha, alphaGamma) or the isobar
+// profile; optional lighting) with the projection factor 1 / (-n.w) taken as
+// 1 (it belongs to the GL camera, which has no headless counterpart), then
+// times alpha.
+__global__ void k_slices(View V, Tex tex, Tex grad, uchar4* out) {
+    int const px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= V.width || py >= V.height) return;
+    int const axis = V.sliceAxis % 3;
+    bool const towardsPlus = V.sliceAxis < 3;
+    int const a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
+    float const u = (px + .5f) / V.width, v = (py + .5f) / V.height;
+    int const n = V.numSlices;
+    float rgb[3] = {0.f, 0.f, 0.f}, acc = 0.f;
+    for (int s = 0; s <= n; ++s) {
+        // back to front: looking towards +axis the back is f = 1
+        int const j = towardsPlus ? n - s : s;
+        float const f = (float)j / (float)n;
+        float c3[3];
+        c3[axis] = f;
+        c3[a1] = u;
+        c3[a2] = v;
+        // with the chart map the identity the world coordinate of a slice
+        // point maps back to these texture coordinates; the slice rotation
+        // is applied about them as the shader does
+        float3 tc = quatRotate(V.q, make_float3(c3[0], c3[1], c3[2]));
+        if (tc.x < 0.f || tc.x > 1.f || tc.y < 0.f || tc.y > 1.f || tc.z < 0.f || tc.z > 1.f) continue;
+        float3 const ng = texToNoGhost(V, tc);
+        auto voxel = [&](float3 q) { return sampleLinear(tex, q.x, q.y, q.z).x; };
+        float const value = voxel(ng);
+        float const frac = gradientFrac(V, value);
+        float4 c = gradientColor(grad, frac);
+        float a;
+        if (V.useIsobars) {
+            float const ff = frac * V.numIsobars + .5f;
+            float const ffrac = ff - floorf(ff);
+            float const th = .1f;
+            a = smoothstepf(0.f, th / 3.f, ffrac) - smoothstepf(2.f / 3.f * th, th, ffrac);
+        } else {
+            a = powf(V.alpha, V.alphaGamma);
+        }
+        if (V.useLighting) {
+            float const h = 1.f / 32.f, ambient = .3f;
+            float gx = voxel(make_float3(ng.x + h, ng.y, ng.z)) - voxel(make_float3(ng.x - h, ng.y, ng.z));
+            float gy = voxel(make_float3(ng.x, ng.y + h, ng.z)) - voxel(make_float3(ng.x, ng.y - h, ng.z));
+            float gz = voxel(make_float3(ng.x, ng.y, ng.z + h)) - voxel(make_float3(ng.x, ng.y, ng.z - h));
+            float const ld = fabsf(gz / sqrtf(gx * gx + gy * gy + gz * gz));
+            float const lum = ambient < ld ? ld : ambient;   // GLSL max(x, y) = x < y ? y : x
+            c.x *= lum;
+            c.y *= lum;
+            c.z *= lum;
+        }
+        float const sa = a * V.alpha;
+        rgb[0] = c.x * sa + rgb[0] * (1.f - sa);
+        rgb[1] = c.y * sa + rgb[1] * (1.f - sa);
+        rgb[2] = c.z * sa + rgb[2] * (1.f - sa);
+        acc = sa * sa + acc * (1.f - sa);
+    }
+    out[(long long)py * V.width + px] = toRGBA8(make_float4(rgb[0], rgb[1], rgb[2], acc));
+}
+
 // vector_lic.glsl:36-107 over the velocity (the 'v' display variable), the
 // noise texture a seeded uniform field (vector_lic.lua:69-88 fills it with
 // math.random).  ds = 1 / noiseSize; chartToNoGhostCoord applies the ghost
@@ -617,9 +685,12 @@ int viz_range(const VizState& st, int var, double out[4], cudaStream_t s) {
 int viz_render(const VizState& st, const hc_render& R, unsigned char* out_dev, cudaStream_t s) {
     if (R.width <= 0 || R.height <= 0 || (long long)R.width * R.height > (1ll << 28))
         return fail(HC_ERR_INVALID, "image size");
-    if (R.mode < HC_RENDER_HEATMAP || R.mode > HC_RENDER_LIC) return fail(HC_ERR_INVALID, "render mode");
+    if (R.mode < HC_RENDER_HEATMAP || R.mode > HC_RENDER_SLICES) return fail(HC_ERR_INVALID, "render mode");
     if (R.var < 0 || R.var >= HC_NUM_DISPLAY_VARS) return fail(HC_ERR_INVALID, "unknown display variable");
-    if (R.mode == HC_RENDER_VOLUME && st.d.dim != 3) return fail(HC_ERR_INVALID, "the volume view needs a 3D grid");
+    if ((R.mode == HC_RENDER_VOLUME || R.mode == HC_RENDER_SLICES) && st.d.dim != 3)
+        return fail(HC_ERR_INVALID, "the volume and slice views need a 3D grid");
+    if (R.mode == HC_RENDER_SLICES && (R.num_slices < 1 || R.num_slices > 4096 || R.slice_axis < 0 || R.slice_axis > 5))
+        return fail(HC_ERR_INVALID, "num_slices / slice_axis");
     if (R.mode == HC_RENDER_LIC && st.d.dim < 2) return fail(HC_ERR_INVALID, "the LIC view needs a 2D or 3D grid");
     if (R.mode != HC_RENDER_HEATMAP && R.max_iter > 4096) return fail(HC_ERR_INVALID, "max_iter");
     viz::Grid const g = grid_of(st);
@@ -668,6 +739,8 @@ int viz_render(const VizState& st, const hc_render& R, unsigned char* out_dev, c
     V.useLighting = R.use_lighting;
     V.licIter = R.lic_iter;
     V.noiseSize = R.noise_size;
+    V.sliceAxis = R.slice_axis;
+    V.numSlices = R.num_slices;
     if (R.mode == HC_RENDER_VOLUME) {
         // camera: at `eye`, looking at the domain's centre, y up
         double c[3], f[3], up[3] = {0, 1, 0}, rt[3], u[3];
@@ -727,6 +800,7 @@ int viz_render(const VizState& st, const hc_render& R, unsigned char* out_dev, c
             viz::k_display<float><<<viz::blocks_for(nfull), 256, 0, s>>>(g, R.var, 0, texBuf);
             viz::Tex tex{texBuf, tw, th, td, 1};
             if (R.mode == HC_RENDER_HEATMAP) viz::k_heatmap<<<grd, blk, 0, s>>>(V, tex, grad, reinterpret_cast<uchar4*>(out_dev));
+            else if (R.mode == HC_RENDER_SLICES) viz::k_slices<<<grd, blk, 0, s>>>(V, tex, grad, reinterpret_cast<uchar4*>(out_dev));
             else viz::k_volume<<<grd, blk, 0, s>>>(V, tex, grad, reinterpret_cast<uchar4*>(out_dev));
         }
         e = cudaGetLastError();
@@ -742,7 +816,7 @@ int viz_render(const VizState& st, const hc_render& R, unsigned char* out_dev, c
 extern "C" int hc_render_defaults(int mode, hc_render* out) {
     using namespace hc;
     if (!out) return fail(HC_ERR_INVALID, "out is NULL");
-    if (mode < HC_RENDER_HEATMAP || mode > HC_RENDER_LIC) return fail(HC_ERR_INVALID, "render mode");
+    if (mode < HC_RENDER_HEATMAP || mode > HC_RENDER_SLICES) return fail(HC_ERR_INVALID, "render mode");
     hc_render r;
     std::memset(&r, 0, sizeof(r));
     r.mode = mode;
@@ -762,6 +836,12 @@ extern "C" int hc_render_defaults(int mode, hc_render* out) {
     r.lic_iter = 10;             // DrawVectorLIC.integralMaxIter, vector_lic.lua:12
     r.noise_size = 1024;         // HydroCLApp.drawVectorLICNoiseSize, app.lua:677
     r.noise_seed = 1;
+    r.slice_axis = 2;            // looking along +z
+    r.num_slices = 255;          // Draw3DSlice.numSlices, 3d_slice.lua
+    if (mode == HC_RENDER_SLICES) {
+        r.use_isobars = 1;       // Draw3DSlice.useIsos
+        r.num_isobars = 20.;     // Draw3DSlice.numIsobars
+    }
     *out = r;
     return HC_OK;
 }

@@ -104,7 +104,7 @@ INIT_KINDS = {"sod": 0, "blast": 1, "quadrant": 2, "kelvin-helmholtz": 3}
 DISPLAY_VARS = ["rho", "m x", "m y", "m z", "m mag", "ETotal", "ePot", "v x", "v y", "v z", "v mag", "P",
                 "eInt", "eKin", "eTotal", "EInt", "EKin", "EPot", "S", "H", "h", "HTotal", "hTotal",
                 "speed of sound", "Mach number", "temperature"]
-RENDER_MODES = {"heatmap": 0, "volume": 1, "lic": 2}
+RENDER_MODES = {"heatmap": 0, "volume": 1, "lic": 2, "slices": 3}
 PALETTES = ["white-rainbow-black", "stripes", "blue", "paraview-red-grey-blue"]
 
 
@@ -117,7 +117,7 @@ class Render(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("alpha_gamma", ctypes.c_double), ("num_isobars", ctypes.c_double),
                 ("max_iter", ctypes.c_int), ("use_isobars", ctypes.c_int), ("use_lighting", ctypes.c_int),
                 ("lic_iter", ctypes.c_int), ("noise_size", ctypes.c_int), ("reserved", ctypes.c_int),
-                ("noise_seed", ctypes.c_ulonglong)]
+                ("noise_seed", ctypes.c_ulonglong), ("slice_axis", ctypes.c_int), ("num_slices", ctypes.c_int)]
 
 
 def display_index(var):
@@ -451,8 +451,9 @@ class Solver:
 
     def render(self, mode="heatmap", var="rho", **kw):
         """An RGBA8 image (height, width, 4) of the state: mode 'heatmap'
-        (2d_heatmap.glsl), 'volume' (volumetric.glsl) or 'lic'
-        (vector_lic.glsl); keyword arguments set hc_render fields."""
+        (2d_heatmap.glsl), 'volume' (volumetric.glsl), 'lic'
+        (vector_lic.glsl) or 'slices' (3d_slice.glsl); keyword arguments set
+        hc_render fields."""
         r = make_render(mode, var=var, **kw)
         out = np.empty((r.height, r.width, 4), dtype=np.uint8)
         _check(self.L.hc_solver_render(self.h, ctypes.byref(r), out.ctypes.data))

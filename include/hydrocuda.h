@@ -377,6 +377,7 @@ int hc_solver_display_range(hc_solver* s, int var, double out[4]);
 #define HC_RENDER_HEATMAP  0   /* a slice of `var` through the palette */
 #define HC_RENDER_VOLUME   1   /* a ray march through a 3D grid */
 #define HC_RENDER_LIC      2   /* line-integral convolution of the velocity, coloured by |v| */
+#define HC_RENDER_SLICES   3   /* 3d_slice.glsl: a stack of slices through a 3D grid, blended back to front */
 
 /* the palettes written out in hydro/draw/palette.lua, in its order */
 #define HC_PALETTE_WHITE_RAINBOW_BLACK 0
@@ -404,10 +405,12 @@ typedef struct hc_render {
     int noise_size;           /* LIC: noise texture edge (drawVectorLICNoiseSize) */
     int reserved;
     unsigned long long noise_seed;   /* LIC: SplitMix64 seed of the noise texture */
+    int slice_axis;           /* slices: view axis 0..2 looking towards +axis, 3..5 towards -axis */
+    int num_slices;           /* slices: numSlices (the stack has num_slices + 1 slices) */
 } hc_render;
 
 /* The reference's defaults for a view (palette 1, identity slice rotation,
- * integralMaxIter 10, noise 1024^2) and a 512 x 512 image. */
+ * integralMaxIter 10, noise 1024^2, 255 slices, alpha .15) and a 512 x 512 image. */
 int hc_render_defaults(int mode, hc_render* out);
 /* Renders the solver's state into rgba (host, width * height * 4 bytes). */
 int hc_solver_render(hc_solver* s, const hc_render* r, unsigned char* rgba);

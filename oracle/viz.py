@@ -362,3 +362,55 @@ def volume(tex, n, mins, maxs, width, height, vmin, vmax, eye, fov_y=45., palett
     img = to_rgba8(np.concatenate([rgb, (f32(1) - ra)[..., None]], axis=-1))
     img[~hit] = 0
     return img
+
+
+def slices(tex, n, width, height, vmin, vmax, axis=2, num_slices=255, palette=0, alpha=.15, alpha_gamma=1.,
+           use_isobars=True, num_isobars=20., use_lighting=False, q=(0, 0, 0, 1), use_log=False):
+    """3d_slice.lua's slice stack as an orthographic view along `axis` (0..2
+    towards +axis, 3..5 towards -axis), blended back to front with
+    (SRC_ALPHA, ONE_MINUS_SRC_ALPHA); per slice 3d_slice.glsl's fragment with
+    the projection factor taken as 1."""
+    f32 = np.float32
+    fr = _Frame(3, n, [0, 0, 0], [1, 1, 1])
+    grad = gradient_texture(palette)
+    ax = axis % 3
+    plus = axis < 3
+    a1, a2 = (1 if ax == 0 else 0), (1 if ax == 2 else 2)
+    py, px = np.mgrid[0:height, 0:width].astype(f32)
+    u, v = (px + f32(.5)) / f32(width), (py + f32(.5)) / f32(height)
+    rgb = np.zeros(u.shape + (3,), dtype=f32)
+    acc = np.zeros_like(u)
+
+    def voxel(q3):
+        with np.errstate(all="ignore"):
+            return sample_linear(tex[..., None], q3[0], q3[1], q3[2])[..., 0]
+
+    for s in range(num_slices + 1):
+        j = num_slices - s if plus else s
+        f = f32(j) / f32(num_slices)
+        c = [None, None, None]
+        c[ax] = np.full_like(u, f)
+        c[a1], c[a2] = u, v
+        tx, ty, tz = _quat_rotate(q, c[0], c[1], c[2])
+        inside = ~((tx < 0) | (tx > 1) | (ty < 0) | (ty > 1) | (tz < 0) | (tz > 1))
+        ng = [fr.tex_to_no_ghost(t, k) for k, t in enumerate((tx, ty, tz))]
+        frac = gradient_frac(voxel(ng), vmin, vmax, use_log)
+        col = gradient_color(grad, frac)
+        if use_isobars:
+            ff = frac * f32(num_isobars) + f32(.5)
+            ffrac = ff - np.floor(ff)
+            a = _smoothstep(0., .1 / 3., ffrac) - _smoothstep(2. / 3. * .1, .1, ffrac)
+        else:
+            a = np.full_like(u, f32(alpha) ** f32(alpha_gamma))
+        if use_lighting:
+            h = f32(1. / 32.)
+            gx = voxel([ng[0] + h, ng[1], ng[2]]) - voxel([ng[0] - h, ng[1], ng[2]])
+            gy = voxel([ng[0], ng[1] + h, ng[2]]) - voxel([ng[0], ng[1] - h, ng[2]])
+            gz = voxel([ng[0], ng[1], ng[2] + h]) - voxel([ng[0], ng[1], ng[2] - h])
+            with np.errstate(all="ignore"):
+                g = np.abs(gz / np.sqrt(gx * gx + gy * gy + gz * gz))
+            col = col * np.where(f32(.3) < g, g, f32(.3))[..., None]
+        sa = np.where(inside, a * f32(alpha), f32(0))
+        rgb = np.where(inside[..., None], col[..., :3] * sa[..., None] + rgb * (f32(1) - sa)[..., None], rgb)
+        acc = np.where(inside, sa * sa + acc * (f32(1) - sa), acc)
+    return to_rgba8(np.concatenate([rgb, acc[..., None]], axis=-1))

@@ -96,6 +96,8 @@ def test_render_defaults_without_a_device():
     r = hydrocuda.make_render("heatmap", var="Mach number", palette="blue", width=64)
     assert (r.var, r.palette, r.width) == (hydrocuda.DISPLAY_VARS.index("Mach number"), 2, 64)
     L = hydrocuda.load_library()
+    r = hydrocuda.make_render("slices")
+    assert (r.num_slices, r.use_isobars, r.num_isobars, r.alpha) == (255, 1, 20.0, .15)
     assert L.hc_render_defaults(7, ctypes.byref(hydrocuda.Render())) == -1
     with pytest.raises(ValueError):
         hydrocuda.make_render("heatmap", var="vorticity")

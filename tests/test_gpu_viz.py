@@ -145,10 +145,25 @@ def test_volume(hc, ctx, isobars, lighting):
     assert got[..., 3].max() > 0
 
 
+@pytest.mark.parametrize("axis,isobars", [(2, True), (3, False), (1, True)])
+def test_slices(hc, ctx, axis, isobars):
+    args = cases.c3_blast(12)
+    s = _solver(hc, ctx, args, "blast", "f32", steps=3)
+    U = _grid(s)
+    tex = viz.display_buffer(U, "P", _gamma(args)).astype(np.float32)
+    got = s.render("slices", var="P", width=36, height=30, slice_axis=axis, num_slices=40, use_isobars=isobars,
+                   value_min=.1, value_max=1.)
+    want = viz.slices(tex, s.gridSize, 36, 30, .1, 1., axis=axis, num_slices=40, use_isobars=isobars)
+    _close_images(got, want, frac=.99, tol=3)
+    assert got[..., 3].max() > 0
+
+
 def test_render_rejects_bad_views(hc, ctx):
     s = _solver(hc, ctx, cases.c4_quadrant(16), "quadrant", "f32", steps=0)
     with pytest.raises(hc.HydroCudaError):
         s.render("volume")                 # 2D grid
+    with pytest.raises(hc.HydroCudaError):
+        s.render("slices")                 # 2D grid
     with pytest.raises(hc.HydroCudaError):
         s.render("heatmap", width=0)
     with pytest.raises(hc.HydroCudaError):

@@ -1,7 +1,8 @@
 --[[
 A 'cuda' finite-volume solver for hydro-cl-lua: same args table as
-hydro/solver/fvsolver.lua (eqn='euler', flux='roe', 'hll' or 'rusanov',
-coord='cartesian'), with the update -- boundary, calcLR ("plm cons"), calcFlux,
+hydro/solver/fvsolver.lua (eqn='euler', flux='roe', 'hll', 'rusanov' or
+'euler-hllc', coord='cartesian'), with the update -- boundary, calcLR ("plm
+cons", "plm prim", "plm athena"), calcFlux,
 calcDerivFromFlux,
 the integrator's multAdd sequence, constrainU, calcDT -- run by libhydrocuda on
 one GPU instead of by the OpenCL kernels.
@@ -46,7 +47,7 @@ local function descFromSolver(self, args)
 	for _,xi in ipairs{'x','y','z'} do
 		for _,mm in ipairs{'min','max'} do
 			d.boundary[k] = assert(hc.boundaryIndex[self.boundaryMethods[xi..mm].name],
-				"the cuda solver provides periodic, mirror, freeflow and none boundaries")
+				"the cuda solver provides none, periodic, mirror, freeflow, linear and quadratic boundaries")
 			k = k + 1
 		end
 	end

@@ -49,6 +49,32 @@ int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long lo
 int hc_solver_get_time(hc_solver* s, double* t);
 int hc_solver_set_time(hc_solver* s, double t);
 int hc_solver_status(hc_solver* s);
+typedef struct hc_render {
+	int mode;
+	int var;
+	int width, height;
+	int palette;
+	int use_log;
+	double value_min, value_max;
+	double bbox[4];
+	double slice_angle[4];
+	double fixed_z;
+	double eye[3];
+	double fov_y;
+	double alpha, alpha_gamma, num_isobars;
+	int max_iter;
+	int use_isobars, use_lighting;
+	int lic_iter;
+	int noise_size;
+	int reserved;
+	unsigned long long noise_seed;
+	int slice_axis;
+	int num_slices;
+} hc_render;
+int hc_solver_display(hc_solver* s, int var, int zero_border, double* out);
+int hc_solver_display_range(hc_solver* s, int var, double out[4]);
+int hc_render_defaults(int mode, hc_render* out);
+int hc_solver_render(hc_solver* s, const hc_render* r, unsigned char* rgba);
 ]]
 
 local here = debug.getinfo(1, 'S').source:match'^@(.*)/[^/]*$' or '.'
@@ -77,6 +103,7 @@ M.fluxIndex = {roe = 0, hll = 1, rusanov = 2, ['euler-hllc'] = 3}
 M.reconIndex = {['piecewise constant'] = 1, ['plm cons'] = 2, ['plm prim'] = 3, ['plm athena'] = 4}
 M.precisionIndex = {['f64 plain'] = 0, f64 = 1, f32 = 2}
 M.LAYOUT_AOS6_F64 = 0
+M.renderMode = {heatmap = 0, volume = 1, lic = 2, slices = 3}
 
 function M.check(code)
 	if code ~= 0 then

@@ -35,6 +35,7 @@ SOURCES = {
     "hc_fused_f32_d2b.cu": FAST,
     "hc_fused_f32_d2c.cu": FAST,
     "hc_fused_f32_d2d.cu": FAST,
+    "hc_fused_f32_d2e.cu": FAST,
     "hc_fused_f32_flux.cu": FAST,
     "hc_fused_f32_recon.cu": FAST,
     "hc_fused_f32_d3.cu": FAST,

@@ -17,7 +17,7 @@ void register_f32_d2e(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& 
     // 10: 32x32, 128 threads, 4 CTAs per SM
     // 11: 64x16, 128 threads, 4 CTAs per SM
     // 12: 32x64, 256 threads, 2 CTAs per SM
-    add_plm_pair<T, P, 2, 10, 32, 32, 1, 8, 128, 2, 4>(st);
+    add_plm_set<T, P, 2, 10, 32, 32, 1, 8, 128, 2, 4>(st);   // every compiled-in limiter
     add_plm_pair<T, P, 2, 11, 64, 16, 1, 8, 128, 2, 4>(st);
     add_plm_pair<T, P, 2, 12, 32, 64, 1, 8, 256, 2, 2>(st);
 }

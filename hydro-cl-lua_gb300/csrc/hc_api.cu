@@ -1,6 +1,7 @@
 // hc_api.cu -- the extern "C" entry points declared in include/hydrocuda.h.
 #include "hc_internal.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <climits>
@@ -576,7 +577,7 @@ int hc_batch_destroy(hc_batch* b) {
 }
 
 static int batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout, const hc_init* init,
-                       double t_end, long long max_steps, unsigned long long tag, int* slot) {
+                       double t_end, long long max_steps, unsigned long long tag, int* slot, int sync = 1) {
     if (!b || !desc || !(cons || init) || !slot) return fail(HC_ERR_INVALID, "NULL argument");
     HC_CHECK(validate_desc(desc));
     if (init) HC_CHECK(init_validate(*init, *desc));
@@ -593,7 +594,7 @@ static int batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons
     for (int k = 0; k < b->d.max_slots; ++k)
         if (!b->used[k]) { s = k; break; }
     if (s < 0) return fail(HC_ERR_NO_SLOT, "every slot is in use");
-    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps, 1, init));
+    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps, 1, init, sync));
     b->used[s] = 1;
     b->reported[s] = 0;
     b->tags[s] = tag;
@@ -613,6 +614,28 @@ int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* 
                         double t_end, long long max_steps, unsigned long long tag, int* slot) {
     if (!init) return fail(HC_ERR_INVALID, "NULL argument");
     return batch_admit(b, desc, nullptr, HC_LAYOUT_AOS6_F64, init, t_end, max_steps, tag, slot);
+}
+
+int hc_batch_admit_many(hc_batch* b, int count, const hc_solver_desc* descs, const void* const* cons, int layout,
+                        const double* t_end, const long long* max_steps, const unsigned long long* tags,
+                        int* slots, int* n_admitted) {
+    if (!b || count < 0 || (count > 0 && (!descs || !cons || !slots)) || !n_admitted)
+        return fail(HC_ERR_INVALID, "NULL argument");
+    *n_admitted = 0;
+    for (int k = 0; k < count; ++k) slots[k] = -1;
+    int r = HC_OK;
+    for (int k = 0; k < count && r == HC_OK; ++k) {
+        if (!cons[k]) {
+            r = fail(HC_ERR_INVALID, "NULL argument");
+            break;
+        }
+        r = batch_admit(b, &descs[k], cons[k], layout, nullptr, t_end ? t_end[k] : INFINITY,
+                        max_steps ? max_steps[k] : 0, tags ? tags[k] : (unsigned long long)k, &slots[k], 0);
+        if (r == HC_OK) ++*n_admitted;
+    }
+    // the host buffers are not read after return
+    int const rs = fused_sync(b->fused);
+    return r != HC_OK ? r : rs;
 }
 
 int hc_batch_step(hc_batch* b, int steps, int* n_active) {
@@ -662,6 +685,23 @@ int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout) {
     if (slot < 0 || slot >= b->d.max_slots || !b->used[slot]) return fail(HC_ERR_STATE, "slot not in use");
     HC_CHECK(use_device(b->ctx));
     return fused_get_state(b->fused, slot, cons, layout);
+}
+
+int hc_batch_fetch_many(hc_batch* b, int count, const int* slots, void* const* cons, int layout) {
+    if (!b || count < 0 || (count > 0 && (!slots || !cons))) return fail(HC_ERR_INVALID, "NULL argument");
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    size_t most = 0;
+    for (int k = 0; k < count; ++k) {
+        if (!cons[k]) return fail(HC_ERR_INVALID, "NULL argument");
+        if (slots[k] < 0 || slots[k] >= b->d.max_slots || !b->used[slots[k]]) return fail(HC_ERR_STATE, "slot not in use");
+        most = std::max(most, fused_state_bytes(b->fused, slots[k], layout));
+    }
+    HC_CHECK(use_device(b->ctx));
+    HC_CHECK(fused_reserve_staging(b->fused, most));
+    int r = HC_OK;
+    for (int k = 0; k < count && r == HC_OK; ++k) r = fused_get_state(b->fused, slots[k], cons[k], layout, 0);
+    int const rs = fused_sync(b->fused);
+    return r != HC_OK ? r : rs;
 }
 
 int hc_batch_retire(hc_batch* b, int slot) {

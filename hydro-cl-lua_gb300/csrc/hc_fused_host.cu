@@ -151,7 +151,12 @@ struct FusedSet {
     DevInst* d_inst = nullptr;
     DevCtl* d_ctl = nullptr;
     CUtensorMap* d_tmaps = nullptr;
-    std::vector<CUtensorMap> h_tmaps;
+    // pinned host sources of the per-slot uploads (tensor maps, DevInst,
+    // DevCtl), so that the copies are asynchronous; an entry is rewritten only
+    // after the stream has drained the copy that last read it
+    CUtensorMap* h_tmaps = nullptr;
+    DevInst* h_inst_up = nullptr;
+    DevCtl* h_ctl_up = nullptr;
     int* d_err = nullptr;
     DevCtl* h_ctl = nullptr;       // pinned mirror
     double* d_partial = nullptr;
@@ -242,8 +247,6 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&f->num_sms, cudaDevAttrMultiProcessorCount, dev);
     f->slots.resize(max_slots);
-    f->h_tmaps.resize((size_t)max_slots * kMaxBufs);
-    std::memset(f->h_tmaps.data(), 0, f->h_tmaps.size() * sizeof(CUtensorMap));
     int r = HC_OK;
     auto A = [&](void** p, size_t b) {
         if (r != HC_OK) return;
@@ -256,10 +259,16 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
     A((void**)&f->d_err, sizeof(int));
     A((void**)&f->d_nitems, sizeof(int) * 3);
     A((void**)&f->d_partial, sizeof(double) * 5 * 1024);
-    if (r == HC_OK) {
-        cudaError_t e = cudaMallocHost((void**)&f->h_ctl, sizeof(DevCtl) * max_slots);
+    auto H = [&](void** p, size_t b) {
+        if (r != HC_OK) return;
+        cudaError_t e = cudaMallocHost(p, b);
         if (e != cudaSuccess) r = cuda_fail(e, "cudaMallocHost");
-    }
+        else std::memset(*p, 0, b);
+    };
+    H((void**)&f->h_ctl, sizeof(DevCtl) * max_slots);
+    H((void**)&f->h_tmaps, sizeof(CUtensorMap) * kMaxBufs * max_slots);
+    H((void**)&f->h_inst_up, sizeof(DevInst) * max_slots);
+    H((void**)&f->h_ctl_up, sizeof(DevCtl) * max_slots);
     if (r == HC_OK) {
         cudaMemsetAsync(f->d_inst, 0, sizeof(DevInst) * max_slots, stream);
         cudaMemsetAsync(f->d_ctl, 0, sizeof(DevCtl) * max_slots, stream);
@@ -291,6 +300,9 @@ void fused_destroy(FusedSet* f) {
     cudaFree(f->staging);
     for (int d = 0; d < 3; ++d) cudaFree(f->d_items[d]);
     if (f->h_ctl) cudaFreeHost(f->h_ctl);
+    if (f->h_tmaps) cudaFreeHost(f->h_tmaps);
+    if (f->h_inst_up) cudaFreeHost(f->h_inst_up);
+    if (f->h_ctl_up) cudaFreeHost(f->h_ctl_up);
     if (f->graph) cudaGraphExecDestroy(f->graph);
     delete f;
 }
@@ -437,22 +449,30 @@ int fused_get_state_dev(FusedSet* f, int slot, void* dev, int layout) {
     return HC_OK;
 }
 
-int fused_get_state(FusedSet* f, int slot, void* host, int layout) {
+int fused_get_state(FusedSet* f, int slot, void* host, int layout, int sync) {
     Slot& S = f->slots[slot];
     if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
     const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
     size_t const bytes = layout_bytes(S.cells, layout);
+    // one staging buffer serves every queued fetch: each gather waits in
+    // stream order for the previous copy out of it
     HC_CHECK(ensure_staging(f, bytes));
     A->xfer(f->d_inst, slot, state_buf(f, slot), f->staging, layout, 1, f->stream);
     HC_CUDA(cudaGetLastError());
     HC_CUDA(cudaMemcpyAsync(host, f->staging, bytes, cudaMemcpyDeviceToHost, f->stream));
-    HC_CUDA(cudaStreamSynchronize(f->stream));
+    if (sync) HC_CUDA(cudaStreamSynchronize(f->stream));
     return HC_OK;
 }
 
+size_t fused_state_bytes(const FusedSet* f, int slot, int layout) {
+    return layout_bytes(f->slots[slot].cells, layout);
+}
+
+int fused_reserve_staging(FusedSet* f, size_t bytes) { return ensure_staging(f, bytes); }
+
 int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout, double t_end, long long max_steps,
-              int stop_on_error, const hc_init* init) {
+              int stop_on_error, const hc_init* init, int sync) {
     if (slot < 0 || slot >= f->max_slots || f->slots[slot].used) return fail(HC_ERR_STATE, "slot unavailable");
     HC_CHECK(validate(f, d));
     Slot& S = f->slots[slot];
@@ -517,8 +537,9 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     for (int b = 0; b < nb; ++b, p += planeBytes * 5) I.buf[b] = p;
     for (int b = 0; b < nd; ++b, p += planeBytes * 5) I.dbuf[b] = p;
     S.used = true;
-    HC_CUDA(cudaMemcpyAsync(f->d_inst + slot, &I, sizeof(DevInst), cudaMemcpyHostToDevice, f->stream));
-    DevCtl c;
+    f->h_inst_up[slot] = I;
+    HC_CUDA(cudaMemcpyAsync(f->d_inst + slot, &f->h_inst_up[slot], sizeof(DevInst), cudaMemcpyHostToDevice, f->stream));
+    DevCtl& c = f->h_ctl_up[slot];
     std::memset(&c, 0, sizeof(c));
     c.dtmin[0] = c.dtmin[1] = kInfBits;
     c.active = 1;
@@ -531,7 +552,7 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
         return r;
     }
     f->items_dirty = true;
-    HC_CUDA(cudaStreamSynchronize(f->stream));
+    if (sync) HC_CUDA(cudaStreamSynchronize(f->stream));
     return HC_OK;
 }
 
@@ -544,9 +565,7 @@ int fused_remove(FusedSet* f, int slot) {
     f->pool.release(S.mem, S.bytes);
     S.mem = nullptr;
     S.used = false;
-    DevCtl c;
-    std::memset(&c, 0, sizeof(c));
-    HC_CUDA(cudaMemcpyAsync(f->d_ctl + slot, &c, sizeof(DevCtl), cudaMemcpyHostToDevice, f->stream));
+    HC_CUDA(cudaMemsetAsync(f->d_ctl + slot, 0, sizeof(DevCtl), f->stream));
     f->items_dirty = true;
     return HC_OK;
 }
@@ -861,8 +880,8 @@ int fused_sync(FusedSet* f) {
 }
 
 // ---------------------------------------------------------------------------
-// autotuner: time the first stage of the plan for each tile-shape candidate
-// on the current work list and keep the fastest per dimension
+// autotuner: time whole steps of the live instances with each candidate
+// schedule and keep the fastest per dimension
 // ---------------------------------------------------------------------------
 
 static std::string tune_key(const FusedSet* f, int dim, long long cells) {
@@ -875,8 +894,10 @@ static std::string tune_key(const FusedSet* f, int dim, long long cells) {
 }
 
 static void reencode_all(FusedSet* f, int dim) {
+    cudaStreamSynchronize(f->stream);   // the copies that read the old maps are done
     for (int s = 0; s < f->max_slots; ++s)
         if (f->slots[s].used && f->slots[s].dim == dim) encode_maps(f, s);
+    cudaStreamSynchronize(f->stream);
 }
 
 int fused_autotune(FusedSet* f, const char* cache_path) {

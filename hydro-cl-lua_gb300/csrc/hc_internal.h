@@ -126,8 +126,10 @@ size_t fused_instance_bytes(const FusedSet* f, const hc_solver_desc& d);
 // single-solver form steps on like the reference and only records the status.
 // The initial state comes from `host` (in `layout`), else from `init` (built
 // on the device), else it stays zero until a set_state.
+// sync = 0 leaves the uploads and launches queued (the caller synchronises
+// before the host buffer is reused).
 int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout,
-              double t_end, long long max_steps, int stop_on_error, const hc_init* init = nullptr);
+              double t_end, long long max_steps, int stop_on_error, const hc_init* init = nullptr, int sync = 1);
 int fused_remove(FusedSet* f, int slot);
 int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int reset);
 // resetState from a device-built initial condition
@@ -150,7 +152,10 @@ int viz_render(const VizState& st, const hc_render& r, unsigned char* out_dev, c
 // initial conditions (hc_init.cu): the interior in AoS-6 FP64, x fastest, into device memory
 int init_validate(const hc_init& ic, const hc_solver_desc& d);
 int init_fill(const hc_init& ic, const hc_solver_desc& d, double* dst, cudaStream_t s);
-int fused_get_state(FusedSet* f, int slot, void* host, int layout);
+// sync = 0 leaves the copy queued (the caller synchronises before reading)
+int fused_get_state(FusedSet* f, int slot, void* host, int layout, int sync = 1);
+size_t fused_state_bytes(const FusedSet* f, int slot, int layout);
+int fused_reserve_staging(FusedSet* f, size_t bytes);
 // Runs `steps` updates of every live instance (device-side completion tests).
 int fused_steps(FusedSet* f, int steps);
 int fused_steps_timed(FusedSet* f, int steps, double* stage_ms, int n_stage_ms, double* total_ms);

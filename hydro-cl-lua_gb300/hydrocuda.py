@@ -165,6 +165,10 @@ PROTOTYPES = {
     "hc_batch_step_timed": (_ip, [_vp, _ip, _dp, _ip, _dp]),
     "hc_batch_poll": (_ip, [_vp, ctypes.POINTER(Done), _ip, ctypes.POINTER(ctypes.c_int)]),
     "hc_batch_fetch": (_ip, [_vp, _ip, _vp, _ip]),
+    "hc_batch_admit_many": (_ip, [_vp, _ip, ctypes.POINTER(SolverDesc), ctypes.POINTER(_vp), _ip, _dp,
+                                  ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_ulonglong),
+                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "hc_batch_fetch_many": (_ip, [_vp, _ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(_vp), _ip]),
     "hc_batch_retire": (_ip, [_vp, _ip]),
     "hc_batch_stats_get": (_ip, [_vp, ctypes.POINTER(BatchStats)]),
     "hc_batch_conservation": (_ip, [_vp, _ip, _dp]),
@@ -553,6 +557,39 @@ class Batch:
         self.slot_desc[slot.value] = desc
         return slot.value
 
+    def admit_many(self, items, layout="aos6"):
+        """Admits every (args, cons, t_end, max_steps, tag) of `items` in one
+        call (hc_batch_admit_many: one wait for all uploads).  Returns their
+        slots; on a refusal raises HydroCudaError with `.slots` = the slots of
+        the instances admitted before it (they stay admitted)."""
+        n = len(items)
+        descs = (SolverDesc * n)()
+        ptrs = (_vp * n)()
+        t_end = (ctypes.c_double * n)()
+        steps = (ctypes.c_longlong * n)()
+        tags = (ctypes.c_ulonglong * n)()
+        keep = []
+        for k, (args, cons, te, ms, tag) in enumerate(items):
+            a = dict(self.scheme)
+            a.update(args)
+            descs[k] = make_desc(a)
+            arr = _as_layout(cons, layout, interior_count(descs[k]))
+            keep.append(arr)
+            ptrs[k] = arr.ctypes.data
+            t_end[k], steps[k], tags[k] = float(te), int(ms), int(tag)
+        slots = (ctypes.c_int * max(n, 1))()
+        got = ctypes.c_int(0)
+        code = self.L.hc_batch_admit_many(self.h, n, descs, ptrs, LAYOUTS[layout], t_end, steps, tags, slots,
+                                          ctypes.byref(got))
+        out = [slots[k] for k in range(got.value)]
+        for k, slot in enumerate(out):
+            self.slot_desc[slot] = SolverDesc.from_buffer_copy(descs[k])
+        if code != HC_OK:
+            err = HydroCudaError(code, _lib.hc_last_error().decode())
+            err.slots = out
+            raise err
+        return out
+
     def admit_init(self, args, kind, t_end, max_steps=0, tag=0, **params):
         """admit with the initial condition built on the device (see make_init)."""
         a = dict(self.scheme)
@@ -619,6 +656,27 @@ class Batch:
                 np.dtype(dtype).name, shape[0] * shape[1]))
         _check(self.L.hc_batch_fetch(self.h, int(slot), out.ctypes.data, LAYOUTS[layout]))
         return out
+
+    def fetch_many(self, slots, layout="aos6", outs=None):
+        """fetch of every slot in one call (hc_batch_fetch_many: one wait for
+        all copies); `outs` as fetch's `out`, one per slot, or None."""
+        n = len(slots)
+        shapes = []
+        for slot in slots:
+            # a slot not in use is refused by the library, before any copy
+            m = interior_count(self.slot_desc[slot]) if slot in self.slot_desc else 1
+            shapes.append({"aos6": ((m, 6), np.float64), "soa5": ((5, m), np.float64),
+                           "soa5_f32": ((5, m), np.float32)}[layout])
+        if outs is None:
+            outs = [np.empty(sh, dtype=dt) for sh, dt in shapes]
+        for o, (sh, dt) in zip(outs, shapes):
+            if o.dtype != dt or o.size != sh[0] * sh[1] or not o.flags["C_CONTIGUOUS"] or not o.flags["WRITEABLE"]:
+                raise ValueError("fetch_many: each out must be a writeable C-contiguous %s array of %d values" % (
+                    np.dtype(dt).name, sh[0] * sh[1]))
+        cs = (ctypes.c_int * max(n, 1))(*[int(s) for s in slots])
+        ptrs = (_vp * max(n, 1))(*[o.ctypes.data for o in outs])
+        _check(self.L.hc_batch_fetch_many(self.h, n, cs, ptrs, LAYOUTS[layout]))
+        return outs
 
     def retire(self, slot):
         _check(self.L.hc_batch_retire(self.h, int(slot)))

@@ -298,6 +298,16 @@ int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, in
 /* hc_batch_admit with the initial condition built on the device. */
 int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* init,
                         double t_end, long long max_steps, unsigned long long tag, int* slot);
+/* `count` hc_batch_admit calls in one: instance k from descs[k], cons[k],
+ * t_end[k], max_steps[k], tags[k] (t_end, max_steps, tags may be NULL: +inf,
+ * no limit, k), all in `layout`.  The uploads and set-up launches of every
+ * instance are queued back to back and waited for once, so with pinned host
+ * buffers the host's launch work overlaps the device's copies.  Stops at the
+ * first refusal or error and returns it; *n_admitted = the instances admitted
+ * before it (they stay admitted), slots[k] their slots, -1 for the rest. */
+int hc_batch_admit_many(hc_batch* b, int count, const hc_solver_desc* descs, const void* const* cons, int layout,
+                        const double* t_end, const long long* max_steps, const unsigned long long* tags,
+                        int* slots, int* n_admitted);
 /* Advances every live instance by up to `steps` updates (each instance with its
  * own CFL dt), in batched launches.  *n_active = instances still stepping. */
 int hc_batch_step(hc_batch* b, int steps, int* n_active);
@@ -311,6 +321,10 @@ int hc_batch_step_timed(hc_batch* b, int steps, double* stage_ms, int n_stage_ms
 int hc_batch_poll(hc_batch* b, hc_done* out, int cap, int* n_out);
 /* Copies a slot's interior state to the host. */
 int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout);
+/* `count` hc_batch_fetch calls in one (slot slots[k] into cons[k], all in
+ * `layout`), queued back to back and waited for once.  Checks every slot
+ * before copying anything. */
+int hc_batch_fetch_many(hc_batch* b, int count, const int* slots, void* const* cons, int layout);
 /* Frees a slot and returns its bytes to the budget. */
 int hc_batch_retire(hc_batch* b, int slot);
 int hc_batch_stats_get(hc_batch* b, hc_batch_stats* out);

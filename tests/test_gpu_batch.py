@@ -221,3 +221,82 @@ def test_served_stream_results_match_alone(hc, ctx):
         ref, n, t = alone(hc, ctx, args, cons, t_end, "f32")
         assert r.status == 0 and r.steps == n
         np.testing.assert_array_equal(r.result, ref)
+
+
+@pytest.mark.parametrize("layout", ["soa5_f32", "aos6"])
+def test_admit_many_and_fetch_many_same_bits_as_one_by_one(hc, ctx, layout):
+    """hc_batch_admit_many / hc_batch_fetch_many queue the same uploads,
+    set-up launches and copies as the one-at-a-time calls, with one wait:
+    the same slots, tags and bits, from pinned and from pageable host memory."""
+    import ctypes
+    work = [quad(hc, n, 40 + n) for n in (33, 64, 50, 97, 128)]
+    conv = (lambda a, c: np.ascontiguousarray(c.reshape(-1, 6)[:, :5].T, dtype=np.float32)) \
+        if layout == "soa5_f32" else (lambda a, c: c)
+    inputs = [conv(a, c) for a, c in work]
+    # pinned copies of the inputs for the batched call
+    L = hc.load_library()
+    nbytes = sum(u.nbytes for u in inputs)
+    ptr = ctypes.c_void_p()
+    hc._check(L.hc_host_alloc(nbytes, ctypes.byref(ptr)))
+    try:
+        host = np.frombuffer((ctypes.c_char * nbytes).from_address(ptr.value), dtype=np.uint8)
+        pinned, off = [], 0
+        for u in inputs:
+            v = host[off:off + u.nbytes].view(u.dtype).reshape(u.shape)
+            v[...] = u
+            pinned.append(v)
+            off += u.nbytes
+        got = {}
+        for form in ("one", "many"):
+            b = hc.Batch(ctx, precision="f32", max_slots=8, **SCHEME)
+            if form == "one":
+                slots = [b.admit(a, u, 0.02, max_steps=7, tag=10 + k, layout=layout)
+                         for k, ((a, _), u) in enumerate(zip(work, inputs))]
+            else:
+                slots = b.admit_many([(a, u, 0.02, 7, 10 + k) for k, ((a, _), u) in enumerate(zip(work, pinned))],
+                                     layout=layout)
+            assert slots == list(range(len(work)))
+            for _ in range(20):
+                if b.step(4) == 0:
+                    break
+            done = {ev["tag"]: ev["slot"] for ev in b.poll()}
+            assert sorted(done) == [10 + k for k in range(len(work))]
+            order = [done[10 + k] for k in range(len(work))]
+            if form == "one":
+                got[form] = [b.fetch(s, layout) for s in order]
+            else:
+                outs = [np.empty_like(u) for u in inputs]
+                got[form] = b.fetch_many(order, layout, outs)
+                # the batched fetch into the pinned buffers too
+                b.fetch_many(order, layout, pinned)
+                for x, y in zip(pinned, outs):
+                    np.testing.assert_array_equal(x.reshape(y.shape), y)
+            b.close()
+        for x, y in zip(got["one"], got["many"]):
+            np.testing.assert_array_equal(np.asarray(x).reshape(y.shape), y)
+    finally:
+        L.hc_host_free(ptr)
+
+
+def test_admit_many_stops_at_the_first_refusal(hc, ctx):
+    """A refusal inside admit_many leaves the instances before it admitted
+    (reported in the error's .slots) and admits none after it."""
+    args, cons = quad(hc, 64, 1)
+    probe = hc.Batch(ctx, precision="f32", max_slots=4, **SCHEME)
+    probe.admit(args, cons, 1.0)
+    one = probe.stats()["bytes_in_use"]
+    probe.close()
+    b = hc.Batch(ctx, precision="f32", max_slots=8, hbm_budget=2 * one + one // 2, **SCHEME)
+    with pytest.raises(hc.HydroCudaError) as e:
+        b.admit_many([(args, cons, 1.0, 0, k) for k in range(4)])
+    assert e.value.code == -4
+    assert e.value.slots == [0, 1]
+    assert b.stats()["occupied"] == 2
+    assert b.stats()["bytes_in_use"] == 2 * one
+    # an unknown slot in fetch_many is refused before anything is copied
+    with pytest.raises(hc.HydroCudaError) as e:
+        b.fetch_many([0, 5])
+    assert e.value.code == -8
+    out = b.fetch_many([1, 0])
+    np.testing.assert_array_equal(out[0], b.fetch(1))
+    b.close()

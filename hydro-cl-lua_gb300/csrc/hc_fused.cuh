@@ -1290,6 +1290,44 @@ __global__ void k_xfer(const DevInst* inst, int slot, int buf, void* staging, in
     }
 }
 
+// A state set-up in one pass (admission, resetState, setState): staging ->
+// interior with the layout conversion of k_xfer, constrainU when `reset`, the
+// ghosts that copy one interior cell (periodic / mirror / freeflow) and the
+// CFL min of the cell into ctl.dtmin[ctl.par] (reset to +inf beforehand).
+// Every step reads and writes only its own cell's values, so the result is
+// that of k_xfer, k_constrain, k_fill_ghosts and k_calc_dt run in turn; the
+// linear / quadratic ghosts (k_extrap_slot) read neighbours and follow it.
+template <typename T, int DIM, bool EXACT>
+__global__ void k_load_state(const DevInst* inst, DevCtl* ctl, int slot, int buf, const void* staging, int layout,
+                             int reset) {
+    const DevInst& I = inst[slot];
+    TileK<T> K;
+    makeTileK<T>(K, I, nullptr, nullptr, 0, 0);
+    T* base = reinterpret_cast<T*>(I.buf[buf]);
+    long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
+    double m = __longlong_as_double((long long)kInfBits);
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
+        long long const idx = padIndex<DIM>(I, gx, gy, gz);
+        T u[5];
+        for (int f = 0; f < 5; ++f) {
+            if (layout == HC_LAYOUT_AOS6_F64) u[f] = (T)((const double*)staging)[6 * k + f];
+            else if (layout == HC_LAYOUT_SOA5_F64) u[f] = (T)((const double*)staging)[f * n + k];
+            else u[f] = (T)((const float*)staging)[f * n + k];
+        }
+        if (reset) constrainCell<T, EXACT>(u, K);
+        for (int f = 0; f < 5; ++f) base[f * I.plane + idx] = u[f];
+        bool edge = false;
+        int const g[3] = {gx, gy, gz};
+        for (int d = 0; d < DIM; ++d) edge |= g[d] < 2 || g[d] >= I.n[d] - 2;
+        if (edge) scatterGhosts<T, DIM>(I, base, gx, gy, gz, u);
+        m = fmin(m, (double)dtCell<T, EXACT, DIM>(u, K, I));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m < __longlong_as_double((long long)kInfBits))
+        atomicMin(&ctl[slot].dtmin[ctl[slot].par], (unsigned long long)__double_as_longlong(m));
+}
+
 // Kahan-compensated FP64 sums of the 5 fields times the cell volume; one
 // partial per block, combined on the host in block order.
 template <typename T, int DIM>
@@ -1350,7 +1388,13 @@ struct AuxLauncher {
     void (*fill_ghosts)(const DevInst* inst, int slot, int buf, cudaStream_t s);
     void (*constrain)(const DevInst* inst, int slot, int buf, cudaStream_t s);
     void (*calc_dt)(const DevInst* inst, DevCtl* ctl, int slot, int buf, cudaStream_t s);
-    void (*xfer)(const DevInst* inst, int slot, int buf, void* staging, int layout, int dir, cudaStream_t s);
+    // k_xfer over `cells` interior cells
+    void (*xfer)(const DevInst* inst, int slot, int buf, void* staging, int layout, int dir, long long cells,
+                 cudaStream_t s);
+    // k_load_state over `cells` interior cells
+    void (*load)(const DevInst* inst, DevCtl* ctl, int slot, int buf, const void* staging, int layout, int reset,
+                 long long cells, cudaStream_t s);
+    void (*extrap_slot)(const DevInst* inst, int slot, int buf, cudaStream_t s);
     void (*sums)(const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s);
     // linear / quadratic ghosts of a stage's output on every stepping instance of this dimension
     void (*extrap_stage)(const DevInst* inst, const DevCtl* ctl, int nslots, int out_buf, int rot_buf, cudaStream_t s);

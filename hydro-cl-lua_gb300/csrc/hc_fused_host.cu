@@ -393,6 +393,13 @@ static size_t layout_bytes(long long n, int layout) {
          : layout == HC_LAYOUT_SOA5_F64 ? n * 5 * sizeof(double) : n * 5 * sizeof(float);
 }
 
+// the instance has a linear or quadratic side (ghosts from neighbours)
+static bool has_extrap(const Slot& S) {
+    for (int k = 0; k < 2 * S.dim; ++k)
+        if (S.inst.bc[k] == HC_BOUNDARY_LINEAR || S.inst.bc[k] == HC_BOUNDARY_QUADRATIC) return true;
+    return false;
+}
+
 // buffer holding a slot's current state
 static int state_buf(FusedSet* f, int slot) {
     if (!f->rotates) return 0;
@@ -402,7 +409,11 @@ static int state_buf(FusedSet* f, int slot) {
     return rot ? f->rot_buf : 0;
 }
 
-int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int reset) {
+// fresh: the slot's DevCtl was just uploaded in its reset form (time, steps,
+// status zero, active, both dt minima +inf, parity 0, no buffer rotation), so
+// the two control kernels that would write the same values are not launched
+// and the state goes to buffer 0.
+static int set_state(FusedSet* f, int slot, const void* host, int layout, int reset, bool fresh) {
     Slot& S = f->slots[slot];
     if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
@@ -410,18 +421,20 @@ int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int res
     size_t const bytes = layout_bytes(S.cells, layout);
     HC_CHECK(ensure_staging(f, bytes));
     HC_CUDA(cudaMemcpyAsync(f->staging, host, bytes, cudaMemcpyHostToDevice, f->stream));
-    int const b = state_buf(f, slot);
-    if (reset) fz::k_restart<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
-    A->xfer(f->d_inst, slot, b, f->staging, layout, 0, f->stream);
-    if (reset) A->constrain(f->d_inst, slot, b, f->stream);
-    A->fill_ghosts(f->d_inst, slot, b, f->stream);
-    fz::k_reset_dtmin<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
-    A->calc_dt(f->d_inst, f->d_ctl, slot, b, f->stream);
+    int const b = fresh ? 0 : state_buf(f, slot);
+    if (reset && !fresh) fz::k_restart<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
+    if (!fresh) fz::k_reset_dtmin<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
+    A->load(f->d_inst, f->d_ctl, slot, b, f->staging, layout, reset, S.cells, f->stream);
+    if (has_extrap(S)) A->extrap_slot(f->d_inst, slot, b, f->stream);
     HC_CUDA(cudaGetLastError());
     return HC_OK;
 }
 
-int fused_init_state(FusedSet* f, int slot, const hc_init& ic) {
+int fused_set_state(FusedSet* f, int slot, const void* host, int layout, int reset) {
+    return set_state(f, slot, host, layout, reset, false);
+}
+
+static int init_state(FusedSet* f, int slot, const hc_init& ic, bool fresh) {
     Slot& S = f->slots[slot];
     if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
     HC_CHECK(init_validate(ic, S.d));
@@ -429,22 +442,22 @@ int fused_init_state(FusedSet* f, int slot, const hc_init& ic) {
     HC_CHECK(ensure_staging(f, layout_bytes(S.cells, HC_LAYOUT_AOS6_F64)));
     HC_CHECK(init_fill(ic, S.d, static_cast<double*>(f->staging), f->stream));
     // from here on exactly the path of a host upload (fused_set_state with reset)
-    int const b = state_buf(f, slot);
-    fz::k_restart<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
-    A->xfer(f->d_inst, slot, b, f->staging, HC_LAYOUT_AOS6_F64, 0, f->stream);
-    A->constrain(f->d_inst, slot, b, f->stream);
-    A->fill_ghosts(f->d_inst, slot, b, f->stream);
-    fz::k_reset_dtmin<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
-    A->calc_dt(f->d_inst, f->d_ctl, slot, b, f->stream);
+    int const b = fresh ? 0 : state_buf(f, slot);
+    if (!fresh) fz::k_restart<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
+    if (!fresh) fz::k_reset_dtmin<<<1, 1, 0, f->stream>>>(f->d_ctl, slot);
+    A->load(f->d_inst, f->d_ctl, slot, b, f->staging, HC_LAYOUT_AOS6_F64, 1, S.cells, f->stream);
+    if (has_extrap(S)) A->extrap_slot(f->d_inst, slot, b, f->stream);
     HC_CUDA(cudaGetLastError());
     return HC_OK;
 }
+
+int fused_init_state(FusedSet* f, int slot, const hc_init& ic) { return init_state(f, slot, ic, false); }
 
 int fused_get_state_dev(FusedSet* f, int slot, void* dev, int layout) {
     Slot& S = f->slots[slot];
     if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
-    find_aux(f->sch.precision, S.dim)->xfer(f->d_inst, slot, state_buf(f, slot), dev, layout, 1, f->stream);
+    find_aux(f->sch.precision, S.dim)->xfer(f->d_inst, slot, state_buf(f, slot), dev, layout, 1, S.cells, f->stream);
     HC_CUDA(cudaGetLastError());
     return HC_OK;
 }
@@ -458,7 +471,7 @@ int fused_get_state(FusedSet* f, int slot, void* host, int layout, int sync) {
     // one staging buffer serves every queued fetch: each gather waits in
     // stream order for the previous copy out of it
     HC_CHECK(ensure_staging(f, bytes));
-    A->xfer(f->d_inst, slot, state_buf(f, slot), f->staging, layout, 1, f->stream);
+    A->xfer(f->d_inst, slot, state_buf(f, slot), f->staging, layout, 1, S.cells, f->stream);
     HC_CUDA(cudaGetLastError());
     HC_CUDA(cudaMemcpyAsync(host, f->staging, bytes, cudaMemcpyDeviceToHost, f->stream));
     if (sync) HC_CUDA(cudaStreamSynchronize(f->stream));
@@ -545,8 +558,8 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     c.active = 1;
     HC_CUDA(cudaMemcpyAsync(f->d_ctl + slot, &c, sizeof(DevCtl), cudaMemcpyHostToDevice, f->stream));
     int r = encode_maps(f, slot);
-    if (r == HC_OK && host) r = fused_set_state(f, slot, host, layout, 1);
-    if (r == HC_OK && !host && init) r = fused_init_state(f, slot, *init);
+    if (r == HC_OK && host) r = set_state(f, slot, host, layout, 1, true);
+    if (r == HC_OK && !host && init) r = init_state(f, slot, *init, true);
     if (r != HC_OK) {
         fused_remove(f, slot);
         return r;

@@ -76,6 +76,13 @@ void add_plm_pair(std::vector<StageLauncher>& v) {
     add_stage<T, PREC, DIM, VAR, TX, TY, TZ, L, NT, false, HC_RECON_PLM_CONS, false, HC_LIMITER_VAN_LEER_ABS, UNR, OCC, LANES>(v);
 }
 
+// blocks of 256 threads for a grid-stride pass over `cells` cells: one cell
+// per thread up to 1024 blocks
+inline unsigned gridFor(long long cells) {
+    long long const want = (cells + 255) / 256;
+    return (unsigned)(want < 1 ? 1 : (want > 1024 ? 1024 : want));
+}
+
 template <typename T, int PREC, int DIM, bool EXACT>
 void add_aux(std::vector<AuxLauncher>& v) {
     AuxLauncher a;
@@ -95,8 +102,16 @@ void add_aux(std::vector<AuxLauncher>& v) {
     a.calc_dt = [](const DevInst* inst, DevCtl* ctl, int slot, int buf, cudaStream_t s) {
         k_calc_dt<T, DIM, EXACT><<<1024, 256, 0, s>>>(inst, ctl, slot, buf);
     };
-    a.xfer = [](const DevInst* inst, int slot, int buf, void* staging, int layout, int dir, cudaStream_t s) {
-        k_xfer<T, DIM><<<1024, 256, 0, s>>>(inst, slot, buf, staging, layout, dir);
+    a.xfer = [](const DevInst* inst, int slot, int buf, void* staging, int layout, int dir, long long cells,
+                cudaStream_t s) {
+        k_xfer<T, DIM><<<gridFor(cells), 256, 0, s>>>(inst, slot, buf, staging, layout, dir);
+    };
+    a.load = [](const DevInst* inst, DevCtl* ctl, int slot, int buf, const void* staging, int layout, int reset,
+                long long cells, cudaStream_t s) {
+        k_load_state<T, DIM, EXACT><<<gridFor(cells), 256, 0, s>>>(inst, ctl, slot, buf, staging, layout, reset);
+    };
+    a.extrap_slot = [](const DevInst* inst, int slot, int buf, cudaStream_t s) {
+        k_extrap_slot<T, DIM><<<64, 256, 0, s>>>(inst, slot, buf);
     };
     a.sums = [](const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s) {
         k_sums<T, DIM><<<blocks, 256, 0, s>>>(inst, slot, buf, vol, partial);

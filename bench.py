@@ -243,6 +243,8 @@ def main():
                     help="c4: the batched quadrants (the headline); c1 Sod; c2 Kelvin-Helmholtz 1024^2; "
                          "c3 blast 256^3; c5 serving")
     ap.add_argument("--size", type=int, default=0, help="c2 / c3: grid side (default: the configuration's)")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="c2 / c3: only step the FP32 batch --warmup + this many updates (a case for ncu)")
     ap.add_argument("--schedule", type=int, default=-1,
                     help="c4: pin the 2D stage-kernel schedule (autotuner variant number) instead of tuning")
     ap.add_argument("--requests", type=int, default=1000,
@@ -546,7 +548,7 @@ def batch_solve(hc, ctx, args, cons, precision, t_end=math.inf, max_steps=0, chu
         state = b.fetch(slot, "aos6")
         sums1 = b.conservation(slot)
         return dict(state=state, steps=ev[0]["steps"], t=ev[0]["t"], ms=total_ms, status=ev[0]["status"],
-                    sums0=sums0, sums1=sums1, snaps=snaps)
+                    sums0=sums0, sums1=sums1, snaps=snaps, schedule=b.stats()["schedule"][args["dim"] - 1])
     finally:
         b.close()
 
@@ -688,7 +690,7 @@ def run_grid_config(name, a, U0, t_end, max_steps, plain_updates, oracle_updates
         "status": {"f32": r32["status"], "f64": r64["status"]},
         "cpu_baseline": oracle_rate(hc, a, U0, oracle_updates),
         "config": {"cells": cells, "l2": "inputs %s than L2 (%.0f MB per state array)" % (
-            "larger" if cells * 20 > 129e6 else "smaller", cells * 20 / 1e6)},
+            "larger" if cells * 20 > 129e6 else "smaller", cells * 20 / 1e6), "schedule": r32["schedule"]},
     }
     extra["fp64"]["speedup_f32_vs_plain"] = v32 / extra["fp64"]["plain_value"]
     return config_line(name, "cell-updates/s (FP32 fused)", v32, extra)
@@ -702,9 +704,34 @@ def initial_for(hc, a):
     return hc.sod_state(a)
 
 
+def profile_case(args, a, U0):
+    """A short run of the configuration's FP32 stage kernels for an ncu
+    capture (not a bench value): one admission, the schedule of --schedule
+    (else the autotuner's, from its cache file when the key is there), then
+    --warmup + --profile-steps updates.  Prints one line with the device time."""
+    import hydrocuda as hc
+    ctx = hc.Context(0)
+    b = hc.Batch(ctx, precision="f32", max_slots=1, **_scheme(a))
+    try:
+        b.admit(a, U0, t_end=math.inf, tag=0)
+        if args.schedule >= 0:
+            b.set_schedule(a["dim"], args.schedule)
+        else:
+            b.autotune(os.path.join(PKG, "_build", "autotune_single.txt"))
+        b.step(args.warmup)
+        _, ms = b.step_timed(args.profile_steps)
+        print(json.dumps({"profile_case": True, "cells": _cells(a), "steps": args.profile_steps,
+                          "schedule": b.stats()["schedule"][a["dim"] - 1], "ms_per_step": ms / args.profile_steps}))
+    finally:
+        b.close()
+    return 0
+
+
 def run_c2(args):
     import hydrocuda as hc
     a = conf_kh(args.size or 1024)
+    if args.profile_steps:
+        return profile_case(args, a, hc.kelvin_helmholtz_state(a, seed=2))
     return run_grid_config("2D Kelvin-Helmholtz %d^2, plm cons + MC, Roe, RK3-TVD, CFL .4, periodic, 500 steps"
                            % a["gridSize"][0], a, hc.kelvin_helmholtz_state(a, seed=2), math.inf, 500, 10, 2,
                            checkpoints=(1, 10, 50, 100, 200, 300, 400))
@@ -713,6 +740,8 @@ def run_c2(args):
 def run_c3(args):
     import hydrocuda as hc
     a = conf_blast(args.size or 256)
+    if args.profile_steps:
+        return profile_case(args, a, hc.blast_state(a))
     return run_grid_config("3D blast %d^3, plm cons + minmod, Roe, RK2, CFL .3, gamma 5/3, freeflow, t = 0.1"
                            % a["gridSize"][0], a, hc.blast_state(a), 0.1, 0, 3, 1)
 

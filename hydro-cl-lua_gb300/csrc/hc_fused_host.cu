@@ -1015,6 +1015,7 @@ void register_f32_flux(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_recon(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d2e(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_d3c(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -1030,6 +1031,7 @@ void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>
     register_f32_recon(st, aux);
     register_f32_d2e(st, aux);
     register_f32_d3b(st, aux);
+    register_f32_d3c(st, aux);
     register_f32_d3(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);

@@ -343,7 +343,8 @@ def e2e_run(hc, ctx, work, inputs, cells, schedule, tick=8):
     instance from pinned host memory (H2D) in one hc_batch_admit_many call,
     run the configuration's 200 updates, reading every instance's status back
     (D2H) after each call of `tick` updates (the serving loop's tick), fetch
-    every final state (D2H) in one hc_batch_fetch_many call.  Measured beside
+    every final state (D2H) into a second pinned buffer in one
+    hc_batch_fetch_many call.  Measured beside
     it: the same job reading the status after every update, and with one
     admit / fetch call per instance."""
     import ctypes
@@ -351,8 +352,10 @@ def e2e_run(hc, ctx, work, inputs, cells, schedule, tick=8):
     L = hc.load_library()
     ptr = ctypes.c_void_p()
     hc._check(L.hc_host_alloc(nbytes, ctypes.byref(ptr)))
+    optr = ctypes.c_void_p()
+    hc._check(L.hc_host_alloc(nbytes, ctypes.byref(optr)))
 
-    def job(views, per_call, many):
+    def job(views, outs, per_call, many):
         t0 = time.perf_counter()
         b = hc.Batch(ctx, precision="f32", max_slots=len(work), **SCHEME)
         if many:
@@ -371,32 +374,34 @@ def e2e_run(hc, ctx, work, inputs, cells, schedule, tick=8):
         t_step = time.perf_counter()
         evs = b.poll()
         if many:
-            b.fetch_many([ev["slot"] for ev in evs], "soa5_f32", [views[ev["tag"]] for ev in evs])
+            b.fetch_many([ev["slot"] for ev in evs], "soa5_f32", [outs[ev["tag"]] for ev in evs])
         else:
             for ev in evs:
-                b.fetch(ev["slot"], "soa5_f32", out=views[ev["tag"]])
+                b.fetch(ev["slot"], "soa5_f32", out=outs[ev["tag"]])
         t1 = time.perf_counter()
         b.close()
         return t0, t_admit, t_step, t1, len(evs), calls + 1
 
     try:
         host = np.frombuffer((ctypes.c_char * nbytes).from_address(ptr.value), dtype=np.float32)
-        views, off = [], 0
+        ohost = np.frombuffer((ctypes.c_char * nbytes).from_address(optr.value), dtype=np.float32)
+        views, outs, off = [], [], 0
         for u in inputs:
-            v = host[off:off + u.size].reshape(u.shape)
-            views.append(v)
+            views.append(host[off:off + u.size].reshape(u.shape))
+            outs.append(ohost[off:off + u.size].reshape(u.shape))
             off += u.size
+        for v, u in zip(views, inputs):
+            v[...] = u
 
         def run(per_call, many):
-            for v, u in zip(views, inputs):
-                v[...] = u
-            return job(views, per_call, many)
+            return job(views, outs, per_call, many)
 
         t0, t_admit, t_step, t1, got, calls = run(tick, True)
         p0, _, _, p1, _, _ = run(1, True)
         q0, q_admit, q_step, q1, _, _ = run(tick, False)
     finally:
         L.hc_host_free(ptr)
+        L.hc_host_free(optr)
     ctl_bytes = STATUS_BYTES_PER_SLOT * len(work)
     return {"value": cells * E2E_STEPS / (t1 - t0), "unit": UNIT,
             "h2d_bytes_per_step": nbytes / E2E_STEPS, "d2h_bytes_per_step": nbytes / E2E_STEPS + ctl_bytes * calls / E2E_STEPS,

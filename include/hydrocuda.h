@@ -102,7 +102,7 @@ extern "C" {
 #define HC_RECON_PLM_ATHENA          4   /* "plm athena" (plm.cl:782-879, with its L/R assignment) */
 #define HC_NUM_RECONS                5
 
-/* interface flux (hydro/flux/*.lua); the flux limiter applies to Roe only
+/* interface flux (the modules of hydro/flux); the flux limiter applies to Roe only
  * (fvsolver.lua:62-64) */
 #define HC_FLUX_ROE      0   /* "roe" (roe.cl) */
 #define HC_FLUX_HLL      1   /* "hll", waves 'Davis direct bounded' (hll.cl) */

@@ -114,3 +114,21 @@ def test_init_defaults_without_a_device():
     assert L.hc_init_defaults(7, ctypes.byref(ic)) == -1
     q = hydrocuda.make_init("quadrant", q=[(1, 2, 3, 4)] * 4)
     assert list(q.p) == [1, 2, 3, 4] * 4
+
+
+def test_integration_c_examples_compile(tmp_path):
+    """The C snippets of INTEGRATION.md compile against the header, in order in
+    one function (the batch snippet uses the first one's context)."""
+    import subprocess
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```c\n(.*?)```", text, flags=re.S)
+    assert len(blocks) >= 2
+    body = "\n".join(l for b in blocks for l in b.splitlines() if not l.startswith("#include"))
+    src = tmp_path / "snippets.c"
+    src.write_text("\n".join([
+        "#include <stdio.h>", "#include <stddef.h>", '#include "hydrocuda.h"',
+        "void example(double* cons_aos6, int count, const hc_solver_desc* descs, const void* const* states,",
+        "             const long long* max_steps, void** results) {",
+        body, "}"]))
+    subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-Wno-unused-variable", "-fsyntax-only",
+                           "-I", os.path.join(ROOT, "include"), str(src)])

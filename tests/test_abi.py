@@ -64,6 +64,14 @@ def test_bad_arguments_fail_before_the_device():
     assert L.hc_solver_status(None) == -1
     assert L.hc_batch_step(None, 1, None) == -1
     assert b"NULL" in L.hc_last_error()
+    # the batched admission / fetch: a NULL batch or count array is refused
+    got = ctypes.c_int(7)
+    slots = (ctypes.c_int * 2)()
+    assert L.hc_batch_admit_many(None, 2, ctypes.byref(d), None, 0, None, None, None, slots,
+                                 ctypes.byref(got)) == -1
+    assert L.hc_batch_admit_many(None, 0, None, None, 0, None, None, None, None, None) == -1
+    assert L.hc_batch_fetch_many(None, 1, slots, None, 0) == -1
+    assert b"NULL" in L.hc_last_error()
 
 
 def test_descriptor_mapping_follows_reference_names():

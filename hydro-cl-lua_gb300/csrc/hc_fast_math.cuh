@@ -28,13 +28,32 @@ namespace hc {
 namespace fast {
 
 template <typename T> struct M;
+// FP32: the hardware approximations as single instructions (PTX .approx.ftz;
+// the forms without .ftz rescale subnormal arguments around each).  For
+// normal arguments and results both forms give the same value.
 template <> struct M<float> {
-    static __device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
+    static __device__ __forceinline__ float rsqrt_(float x) {
+        float r;
+        asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        return r;
+    }
     static __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
     static __device__ __forceinline__ bool finite_(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
-    static __device__ __forceinline__ float rcp(float x) { return __fdividef(1.f, x); }
-    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
-    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float rcp(float x) {
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        return r;
+    }
+    static __device__ __forceinline__ float div(float a, float b) {
+        float r;
+        asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+        return r;
+    }
+    static __device__ __forceinline__ float sqrt_(float x) {
+        float r;
+        asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        return r;
+    }
     static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
 };
 template <> struct M<double> {

@@ -129,7 +129,13 @@ struct StageArgs {
     int flux;                   // HC_FLUX_*
     int hllcMethod;             // euler-hllc's hllcMethod, 0..2
     int recon;                  // HC_RECON_*
+    int* work;                  // marching kernels: this launch's work counter (zeroed when the step begins)
+    int force_timeout;          // test knob, 0 in normal use: the first wait for each copy counts as run out
 };
+
+// Work counters of the marching kernels: one per (stage, dimension), zeroed by
+// the kernel that begins a step.
+constexpr int kWorkCounters = 4 * 3;
 
 // A slot whose step count left its state in the other buffer of a rotating
 // plan (forward Euler) sees buffers 0 and rot_buf exchanged.
@@ -808,7 +814,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
         // the tile's constants (loads; no FP64 arithmetic) while the tile streams in
         TileK<T> K;
         makeTileK<T>(K, I, ctl, &st, slopeLim, fluxLim, a.flux, a.hllcMethod, a.recon);
-        if (!mbar_wait_bounded(bar, phase, kSpinLimit)) {
+        if (a.force_timeout || !mbar_wait_bounded(bar, phase, kSpinLimit)) {
             // the copy did not complete: record it, give the copy a second
             // bounded chance to land before the CTA releases its smem, stop
             if (tid == 0) { atomicOr(a.err, DEV_TIMEOUT); atomicOr(&ctl->status, DEV_TIMEOUT); }
@@ -1141,7 +1147,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
 
 // Finishes a pending step (t += dt) and begins the next one for every slot:
 // the App's exit test (t >= t_end, before stepping), then dt = cfl * min.
-__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates, BetaTable bt);
+__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates, BetaTable bt, int* work);
 
 template <typename T, int DIM>
 __global__ void k_fill_ghosts(const DevInst* inst, int slot, int buf) {
@@ -1377,6 +1383,8 @@ struct StageLauncher {
     int seg, unroll, min_ctas;   // segment length, sliding-window unroll (0: full), CTAs per SM compiled for
     int lanes;                   // lines per thread (2: packed FP32 pairs)
     int flux;                    // HC_FLUX_* compiled in, or -1 (any: read at run time)
+    int box[3];                  // extents of the TMA box of the stage's input (x, y, z; the fields follow)
+    int march;                   // 1: a marching kernel (one warp per strip item, work counter)
     size_t smem;
     void (*launch)(const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s);
     int (*occupancy)();   // CTAs per SM (sets the smem attribute first); <= 0 on error

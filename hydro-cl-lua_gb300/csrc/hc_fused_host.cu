@@ -19,6 +19,7 @@
 #include <cstddef>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -31,8 +32,9 @@ using namespace fz;
 
 namespace fz {
 
-__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates, BetaTable bt) {
+__global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin, int rotates, BetaTable bt, int* work) {
     int const s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < kWorkCounters) work[s] = 0;   // the marching kernels' work counters of the step's stages
     if (s >= nslots) return;
     DevCtl& c = ctl[s];
     if (c.stepping) {
@@ -61,8 +63,10 @@ __global__ void k_begin(DevCtl* ctl, const DevInst* inst, int nslots, int begin,
 }
 
 // Explicit-dt step of one slot (SolverBase:step(dt): t is not advanced).
-__global__ void k_set_dt(DevCtl* ctl, const DevInst* inst, int slot, double dt, int on, int rotates, BetaTable bt) {
+__global__ void k_set_dt(DevCtl* ctl, const DevInst* inst, int slot, double dt, int on, int rotates, BetaTable bt,
+                         int* work) {
     DevCtl& c = ctl[slot];
+    for (int k = 0; k < kWorkCounters; ++k) work[k] = 0;
     if (on) {
         c.dtmin[c.par ^ 1] = kInfBits;
         c.dt = dt;
@@ -158,6 +162,8 @@ struct FusedSet {
     DevInst* h_inst_up = nullptr;
     DevCtl* h_ctl_up = nullptr;
     int* d_err = nullptr;
+    int* d_work = nullptr;         // [kWorkCounters] work counters of the marching kernels
+    int force_timeout = 0;         // test knob (HC_TEST_FORCE_TIMEOUT at creation): bounded waits count as run out
     DevCtl* h_ctl = nullptr;       // pinned mirror
     double* d_partial = nullptr;
     void* staging = nullptr;
@@ -231,6 +237,11 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
     HC_CHECK(get_encoder());
     FusedSet* f = new FusedSet();
     f->sch = sch;
+    {
+        // test knob for the bounded-wait path; off unless the variable is "1"
+        const char* ft = std::getenv("HC_TEST_FORCE_TIMEOUT");
+        f->force_timeout = ft && ft[0] == '1' && ft[1] == 0;
+    }
     f->esize = sch.precision == HC_F32_FUSED ? 4 : 8;
     f->max_slots = max_slots;
     f->stream = stream;
@@ -257,6 +268,7 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
     A((void**)&f->d_ctl, sizeof(DevCtl) * max_slots);
     A((void**)&f->d_tmaps, sizeof(CUtensorMap) * kMaxBufs * max_slots);
     A((void**)&f->d_err, sizeof(int));
+    A((void**)&f->d_work, sizeof(int) * kWorkCounters);
     A((void**)&f->d_nitems, sizeof(int) * 3);
     A((void**)&f->d_partial, sizeof(double) * 5 * 1024);
     auto H = [&](void** p, size_t b) {
@@ -274,6 +286,7 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
         cudaMemsetAsync(f->d_ctl, 0, sizeof(DevCtl) * max_slots, stream);
         cudaMemsetAsync(f->d_tmaps, 0, sizeof(CUtensorMap) * kMaxBufs * max_slots, stream);
         cudaMemsetAsync(f->d_err, 0, sizeof(int), stream);
+        cudaMemsetAsync(f->d_work, 0, sizeof(int) * kWorkCounters, stream);
         cudaMemsetAsync(f->d_nitems, 0, sizeof(int) * 3, stream);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) r = cuda_fail(e, "cudaMemsetAsync");
@@ -295,6 +308,7 @@ void fused_destroy(FusedSet* f) {
     cudaFree(f->d_ctl);
     cudaFree(f->d_tmaps);
     cudaFree(f->d_err);
+    cudaFree(f->d_work);
     cudaFree(f->d_nitems);
     cudaFree(f->d_partial);
     cudaFree(f->staging);
@@ -349,18 +363,18 @@ static int encode_maps(FusedSet* f, int slot) {
     cuuint32_t box[5], estride[5] = {1, 1, 1, 1, 1};
     size_t const es = f->esize;
     gdim[0] = I.px;
-    box[0] = L->tx + 4;
+    box[0] = L->box[0];
     if (S.dim == 1) {
         gdim[1] = 5; box[1] = 5;
         gstride[0] = I.plane * es;
     } else if (S.dim == 2) {
         gdim[1] = I.py; gdim[2] = 5;
-        box[1] = L->ty + 4; box[2] = 5;
+        box[1] = L->box[1]; box[2] = 5;
         gstride[0] = (cuuint64_t)I.px * es;
         gstride[1] = I.plane * es;
     } else {
         gdim[1] = I.py; gdim[2] = I.pz; gdim[3] = 5;
-        box[1] = L->ty + 4; box[2] = L->tz + 4; box[3] = 5;
+        box[1] = L->box[1]; box[2] = L->box[2]; box[3] = 5;
         gstride[0] = (cuuint64_t)I.px * es;
         gstride[1] = (cuuint64_t)I.px * I.py * es;
         gstride[2] = I.plane * es;
@@ -664,6 +678,8 @@ static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
             a.flux = f->sch.flux;
             a.hllcMethod = f->sch.hllc_method == HC_HLLC_DEFAULT ? 2 : f->sch.hllc_method - 1;
             a.recon = f->sch.recon;
+            a.work = f->d_work + P.stage[s].index * 3 + d;
+            a.force_timeout = f->force_timeout;
             fill_stage(a.st, P.stage[s], P.stage[s].index);
             f->launcher[d]->launch(a, f->sch.slope_limiter, f->sch.flux_limiter, f->grid[d], f->stream);
         }
@@ -679,7 +695,7 @@ static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
 
 static int launch_step(FusedSet* f, int dims_mask) {
     unsigned const g = (unsigned)((f->max_slots + 127) / 128);
-    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates, f->betas);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates, f->betas, f->d_work);
     return launch_stages(f, f->plan[0], dims_mask);
 }
 
@@ -705,7 +721,7 @@ int fused_steps(FusedSet* f, int steps) {
     if (!f->graph_valid) HC_CHECK(capture_graph(f));
     for (int k = 0; k < steps; ++k) HC_CUDA(cudaGraphLaunch(f->graph, f->stream));
     unsigned const g = (unsigned)((f->max_slots + 127) / 128);
-    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas, f->d_work);
     HC_CUDA(cudaGetLastError());
     return HC_OK;
 }
@@ -721,7 +737,7 @@ int fused_steps_timed(FusedSet* f, int steps, double* stage_ms, int n_stage_ms, 
     HC_CUDA(cudaEventRecord(ev[k++], f->stream));
     unsigned const g = (unsigned)((f->max_slots + 127) / 128);
     for (int s = 0; s < steps; ++s) {
-        fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates, f->betas);
+        fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates, f->betas, f->d_work);
         for (int st = 0; st < P.n_stages; ++st) {
             IntegratorPlan one;
             std::memset(&one, 0, sizeof(one));
@@ -732,7 +748,7 @@ int fused_steps_timed(FusedSet* f, int steps, double* stage_ms, int n_stage_ms, 
             HC_CUDA(cudaEventRecord(ev[k++], f->stream));
         }
     }
-    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas, f->d_work);
     HC_CUDA(cudaEventRecord(ev[k++], f->stream));
     HC_CUDA(cudaEventSynchronize(ev[k - 1]));
     size_t j = 1;
@@ -753,9 +769,9 @@ int fused_step_dt(FusedSet* f, int slot, double dt) {
     HC_CHECK(rebuild_items(f));
     const Slot& S = f->slots[slot];
     if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
-    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 1, f->rotates, f->betas);
+    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 1, f->rotates, f->betas, f->d_work);
     HC_CHECK(launch_stages(f, f->plan[0], 1 << (S.dim - 1)));
-    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 0, f->rotates, f->betas);
+    fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 0, f->rotates, f->betas, f->d_work);
     HC_CUDA(cudaGetLastError());
     return HC_OK;
 }
@@ -961,7 +977,7 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
             int const reps = 3;
             for (int r = 0; r < reps; ++r) HC_CHECK(launch_step(f, mask));
             cudaEventRecord(e1, f->stream);
-            fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas);
+            fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 0, f->rotates, f->betas, f->d_work);
             cudaEventSynchronize(e1);
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
@@ -1017,6 +1033,7 @@ void register_f32_d2e(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3c(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_m2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -1033,6 +1050,7 @@ void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>
     register_f32_d3b(st, aux);
     register_f32_d3c(st, aux);
     register_f32_d3(st, aux);
+    register_f32_m2(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);
     register_f64_d3(st, aux);

@@ -4,6 +4,7 @@
 #pragma once
 
 #include "hc_fused.cuh"
+#include "hc_march.cuh"
 
 namespace hc {
 namespace fz {
@@ -37,6 +38,10 @@ void add_stage(std::vector<StageLauncher>& v) {
     sl.min_ctas = K;
     sl.lanes = LANES;
     sl.flux = EXACT ? -1 : FLUX;
+    sl.box[0] = TX + 4;
+    sl.box[1] = DIM > 1 ? TY + 4 : 1;
+    sl.box[2] = DIM > 2 ? TZ + 4 : 1;
+    sl.march = 0;
     sl.smem = Cfg::SMEM;
     sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
         k_stage<T, DIM, TX, TY, TZ, L, NT, EXACT, PLM, LIM, SLOPE, UNR, K, LANES, FLUX><<<grid, NT, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
@@ -46,6 +51,46 @@ void add_stage(std::vector<StageLauncher>& v) {
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NT, Cfg::SMEM) != cudaSuccess) return -1;
+        return n;
+    };
+    v.push_back(sl);
+}
+
+// A 2D marching schedule (hc_march.cuh): NW warps per CTA, segments of H
+// rows, chunks of C rows in NB buffers, the slope limiter SLOPE compiled in
+// (-1: read at run time), OCC CTAs per SM.
+template <int VAR, int NW, int H, int C, int NB, int SLOPE, int OCC>
+void add_march2(std::vector<StageLauncher>& v) {
+    using Cfg = MarchCfg<NW, C, NB>;
+    StageLauncher sl;
+    sl.precision = HC_F32_FUSED;
+    sl.dim = 2;
+    sl.recon = HC_RECON_PLM_CONS;
+    sl.lim = false;
+    sl.slope = SLOPE;
+    sl.variant = VAR;
+    sl.tx = kStripW;
+    sl.ty = H;
+    sl.tz = 1;
+    sl.nthreads = NW * 32;
+    sl.seg = H;
+    sl.unroll = 1;
+    sl.min_ctas = OCC;
+    sl.lanes = 1;
+    sl.flux = HC_FLUX_ROE;
+    sl.box[0] = kMarchBW;
+    sl.box[1] = C;
+    sl.box[2] = 1;
+    sl.march = 1;
+    sl.smem = Cfg::SMEM;
+    sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
+        k_march2<NW, H, C, NB, SLOPE, OCC><<<grid, NW * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+    };
+    sl.occupancy = []() -> int {
+        auto k = k_march2<NW, H, C, NB, SLOPE, OCC>;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NW * 32, Cfg::SMEM) != cudaSuccess) return -1;
         return n;
     };
     v.push_back(sl);

@@ -613,7 +613,9 @@ int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, in
 int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* init,
                         double t_end, long long max_steps, unsigned long long tag, int* slot) {
     if (!init) return fail(HC_ERR_INVALID, "NULL argument");
-    return batch_admit(b, desc, nullptr, HC_LAYOUT_AOS6_F64, init, t_end, max_steps, tag, slot);
+    // no host buffer is read after return: the set-up launches stay queued
+    // behind whatever the batch's stream is running
+    return batch_admit(b, desc, nullptr, HC_LAYOUT_AOS6_F64, init, t_end, max_steps, tag, slot, 0);
 }
 
 int hc_batch_admit_many(hc_batch* b, int count, const hc_solver_desc* descs, const void* const* cons, int layout,
@@ -623,6 +625,7 @@ int hc_batch_admit_many(hc_batch* b, int count, const hc_solver_desc* descs, con
         return fail(HC_ERR_INVALID, "NULL argument");
     *n_admitted = 0;
     for (int k = 0; k < count; ++k) slots[k] = -1;
+    HC_CHECK(use_device(b->ctx));
     int r = HC_OK;
     for (int k = 0; k < count && r == HC_OK; ++k) {
         if (!cons[k]) {
@@ -653,11 +656,50 @@ int hc_batch_step(hc_batch* b, int steps, int* n_active) {
     return HC_OK;
 }
 
+int hc_batch_step_async(hc_batch* b, int steps) {
+    if (!b) return fail(HC_ERR_INVALID, "NULL batch");
+    HC_CHECK(use_device(b->ctx));
+    return fused_steps(b->fused, steps);
+}
+
+int hc_batch_wait(hc_batch* b, int* n_active) {
+    if (!b) return fail(HC_ERR_INVALID, "NULL batch");
+    HC_CHECK(use_device(b->ctx));
+    HC_CHECK(fused_sync(b->fused));
+    if (n_active) {
+        std::vector<SlotInfo> info;
+        HC_CHECK(fused_slot_info(b->fused, info));
+        int n = 0;
+        for (int k = 0; k < b->d.max_slots; ++k) n += b->used[k] && info[k].active;
+        *n_active = n;
+    }
+    return HC_OK;
+}
+
 int hc_batch_step_timed(hc_batch* b, int steps, double* stage_ms, int n_stage_ms, double* total_ms) {
     if (!b || !total_ms || (n_stage_ms > 0 && !stage_ms)) return fail(HC_ERR_INVALID, "NULL argument");
     HC_CHECK(use_device(b->ctx));
     HC_CHECK(fused_steps_timed(b->fused, steps, stage_ms, n_stage_ms, total_ms));
     return fused_sync(b->fused);
+}
+
+int hc_batch_list(hc_batch* b, hc_done* out, int cap, int* n_out) {
+    if (!b || !n_out || (cap > 0 && !out)) return fail(HC_ERR_INVALID, "NULL argument");
+    HC_CHECK(use_device(b->ctx));
+    std::vector<SlotInfo> info;
+    HC_CHECK(fused_slot_info(b->fused, info));
+    int n = 0;
+    for (int k = 0; k < b->d.max_slots && n < cap; ++k) {
+        if (!b->used[k]) continue;
+        out[n].slot = k;
+        out[n].status = info[k].status ? (info[k].status & DEV_TIMEOUT ? HC_ERR_TIMEOUT : HC_ERR_NONFINITE) : HC_OK;
+        out[n].tag = b->tags[k];
+        out[n].steps = info[k].steps;
+        out[n].t = info[k].t;
+        ++n;
+    }
+    *n_out = n;
+    return HC_OK;
 }
 
 int hc_batch_poll(hc_batch* b, hc_done* out, int cap, int* n_out) {

@@ -162,8 +162,11 @@ PROTOTYPES = {
     "hc_batch_admit_init": (_ip, [_vp, ctypes.POINTER(SolverDesc), ctypes.POINTER(Init), ctypes.c_double,
                                   ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_int)]),
     "hc_batch_step": (_ip, [_vp, _ip, ctypes.POINTER(ctypes.c_int)]),
+    "hc_batch_step_async": (_ip, [_vp, _ip]),
+    "hc_batch_wait": (_ip, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "hc_batch_step_timed": (_ip, [_vp, _ip, _dp, _ip, _dp]),
     "hc_batch_poll": (_ip, [_vp, ctypes.POINTER(Done), _ip, ctypes.POINTER(ctypes.c_int)]),
+    "hc_batch_list": (_ip, [_vp, ctypes.POINTER(Done), _ip, ctypes.POINTER(ctypes.c_int)]),
     "hc_batch_fetch": (_ip, [_vp, _ip, _vp, _ip]),
     "hc_batch_admit_many": (_ip, [_vp, _ip, ctypes.POINTER(SolverDesc), ctypes.POINTER(_vp), _ip, _dp,
                                   ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_ulonglong),
@@ -625,6 +628,16 @@ class Batch:
         _check(self.L.hc_batch_step(self.h, int(steps), ctypes.byref(n)))
         return n.value
 
+    def step_async(self, steps=1):
+        """Queues `steps` updates and returns at once (hc_batch_step_async)."""
+        _check(self.L.hc_batch_step_async(self.h, int(steps)))
+
+    def wait(self):
+        """Waits for queued work; returns the instances still stepping (hc_batch_wait)."""
+        n = ctypes.c_int()
+        _check(self.L.hc_batch_wait(self.h, ctypes.byref(n)))
+        return n.value
+
     def step_timed(self, steps=1):
         """Steps with CUDA events around each stage kernel; returns (stage_ms list, total_ms)."""
         n = self.stats()["n_stages"]
@@ -637,6 +650,14 @@ class Batch:
         arr = (Done * cap)()
         n = ctypes.c_int()
         _check(self.L.hc_batch_poll(self.h, arr, cap, ctypes.byref(n)))
+        return [dict(slot=arr[i].slot, status=arr[i].status, tag=arr[i].tag, steps=arr[i].steps, t=arr[i].t)
+                for i in range(n.value)]
+
+    def list(self, cap=4096):
+        """Every occupied slot, finished or not (hc_batch_list): slot, status so far, tag, updates, t."""
+        arr = (Done * cap)()
+        n = ctypes.c_int()
+        _check(self.L.hc_batch_list(self.h, arr, cap, ctypes.byref(n)))
         return [dict(slot=arr[i].slot, status=arr[i].status, tag=arr[i].tag, steps=arr[i].steps, t=arr[i].t)
                 for i in range(n.value)]
 

@@ -1,11 +1,13 @@
 """Continuous-batching request loop over hc_batch (host side).
 
 Requests (Euler solves of any dimension and size, each with its own end time)
-arrive over time.  The loop admits every arrived request it can (FIFO) against
-the batch's HBM budget and slot table, advances all live solves together with
-``hc_batch_step`` (each with its own CFL dt, on the device), and as solves
-finish it fetches their states, retires their slots (returning their bytes to
-the budget) and records time-to-solution.  Requests that arrive while others
+arrive over time.  The loop admits arrived requests against the batch's HBM budget and slot
+table (in arrival order, passing over one that does not fit unless it has
+waited too long), advances all live solves together with
+``hc_batch_step_async`` / ``hc_batch_wait`` (each with its own CFL dt, on the
+device; admissions are issued while a tick runs), and as solves finish it
+fetches their states, retires their slots (returning their bytes to the
+budget) and records time-to-solution.  Requests that arrive while others
 are on the GPU are admitted as soon as memory and a slot free up, so their
 work overlaps on the device with the solves already running.
 
@@ -49,21 +51,69 @@ class Request:
 class Server:
     """Drives one hc_batch with a stream of requests.
 
-    steps_per_tick: updates per hc_batch_step call between admission / poll
-    passes (larger values amortise host round trips, smaller ones admit and
-    retire sooner).  keep_results: fetch the final state of every solve (True),
-    of none (False), or of the requests whose tags are in the given set.
+    steps_per_tick: updates per tick between admission / poll passes (larger
+    values amortise host round trips, smaller ones admit and retire sooner).
+    keep_results: fetch the final state of every solve (True), of none
+    (False), or of the requests whose tags are in the given set.
+
+    Admission backfills: the arrived requests are offered in arrival order and
+    one that does not fit (HBM budget or slot table) is passed over for now,
+    so smaller requests behind it still start.  A request that has waited
+    longer than age_cap_s is not passed over: admission stops at it until
+    retirements free enough memory, so a large request is not starved.  At
+    most max_refusals refusals end the pass (each is a host call).
+
+    async_ticks: each tick's updates are queued first (hc_batch_step_async),
+    then the arrived requests are admitted while they run (the admissions'
+    set-up launches queue behind them), then the tick is waited for and the
+    finished solves are polled, fetched and retired.
     """
 
-    def __init__(self, batch, steps_per_tick=8, keep_results=True, result_layout="aos6"):
+    def __init__(self, batch, steps_per_tick=8, keep_results=True, result_layout="aos6", age_cap_s=1.0,
+                 max_refusals=8, async_ticks=True):
         self.batch = batch
         self.steps_per_tick = int(steps_per_tick)
         self.keep_results = keep_results
         self.result_layout = result_layout
+        self.age_cap_s = float(age_cap_s)
+        self.max_refusals = int(max_refusals)
+        self.async_ticks = bool(async_ticks)
         self.by_tag = {}
         self.slot_of = {}
         self.ticks = 0
         self.cell_updates = 0
+        self.wait_s = 0.0          # host time spent waiting for the device's ticks
+        self.passed_over = 0       # admissions that went ahead of an older waiting request
+
+    def _admit(self, waiting, clock, live, cells_of):
+        """One admission pass over the waiting requests; returns how many started."""
+        i, refused, started = 0, 0, 0
+        while i < len(waiting) and refused < self.max_refusals:
+            r = waiting[i]
+            if r.init is not None:
+                slot = self.batch.try_admit_init(r.args, r.init[0], r.t_end, tag=r.tag, **r.init[1])
+            else:
+                if callable(r.cons):
+                    r.cons = r.cons()
+                slot = self.batch.try_admit(r.args, r.cons, r.t_end, tag=r.tag, layout=r.layout)
+            if slot is None:
+                if live + started == 0:
+                    raise RuntimeError("request %d does not fit an empty batch" % r.tag)
+                refused += 1
+                if clock() - r.arrival > self.age_cap_s:
+                    break          # the oldest starving request keeps its place
+                i += 1
+                continue
+            del waiting[i]
+            if i > 0:
+                self.passed_over += 1
+            r.admitted = clock()
+            r.cons = None
+            self.by_tag[r.tag] = r
+            self.slot_of[r.tag] = slot
+            cells_of[r.tag] = hydrocuda.interior_count(self.batch.slot_desc[slot])
+            started += 1
+        return started
 
     def run(self, requests, clock=None, sleep=None, max_wall=None):
         """Serves `requests` (sorted by arrival time, seconds from start).
@@ -75,36 +125,27 @@ class Server:
         clock = clock or (lambda: time.perf_counter() - t0)
         sleep = sleep or time.sleep
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        waiting = []
         live = 0
         done = []
         cells_of = {}
-        while pending or live:
+        while pending or waiting or live:
             now = clock()
             if max_wall is not None and now > max_wall:
                 break
-            # admit every arrived request that fits
             while pending and pending[0].arrival <= now:
-                r = pending[0]
-                if r.init is not None:
-                    slot = self.batch.try_admit_init(r.args, r.init[0], r.t_end, tag=r.tag, **r.init[1])
+                waiting.append(pending.popleft())
+            ticking = live > 0
+            if ticking and self.async_ticks:
+                self.batch.step_async(self.steps_per_tick)
+            started = self._admit(waiting, clock, live, cells_of)
+            if ticking:
+                w0 = time.perf_counter()
+                if self.async_ticks:
+                    self.batch.wait()
                 else:
-                    if callable(r.cons):
-                        r.cons = r.cons()
-                    slot = self.batch.try_admit(r.args, r.cons, r.t_end, tag=r.tag, layout=r.layout)
-                if slot is None:
-                    if live == 0:
-                        raise RuntimeError("request %d does not fit an empty batch" % r.tag)
-                    break
-                pending.popleft()
-                r.admitted = clock()
-                r.cons = None
-                self.by_tag[r.tag] = r
-                self.slot_of[r.tag] = slot
-                d = self.batch.slot_desc[slot]
-                cells_of[r.tag] = hydrocuda.interior_count(d)
-                live += 1
-            if live:
-                self.batch.step(self.steps_per_tick)
+                    self.batch.step(self.steps_per_tick)
+                self.wait_s += time.perf_counter() - w0
                 self.ticks += 1
                 for ev in self.batch.poll():
                     r = self.by_tag.pop(ev["tag"])
@@ -120,7 +161,8 @@ class Server:
                     self.cell_updates += r.steps * cells_of.pop(r.tag)
                     live -= 1
                     done.append(r)
-            elif pending:
+            live += started
+            if not ticking and not started and pending and not waiting:
                 sleep(max(0.0, pending[0].arrival - clock()))
         return done
 

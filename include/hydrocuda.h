@@ -295,7 +295,9 @@ int hc_batch_destroy(hc_batch* b);
  * every hc_batch_step until t >= t_end or max_steps updates. */
 int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout,
                    double t_end, long long max_steps, unsigned long long tag, int* slot);
-/* hc_batch_admit with the initial condition built on the device. */
+/* hc_batch_admit with the initial condition built on the device.  Reads no
+ * host buffer after return, so it does not wait: the set-up launches queue
+ * behind any hc_batch_step_async in flight. */
 int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* init,
                         double t_end, long long max_steps, unsigned long long tag, int* slot);
 /* `count` hc_batch_admit calls in one: instance k from descs[k], cons[k],
@@ -311,6 +313,14 @@ int hc_batch_admit_many(hc_batch* b, int count, const hc_solver_desc* descs, con
 /* Advances every live instance by up to `steps` updates (each instance with its
  * own CFL dt), in batched launches.  *n_active = instances still stepping. */
 int hc_batch_step(hc_batch* b, int steps, int* n_active);
+/* hc_batch_step without the wait (no counterpart in the reference: the serving
+ * loop's tick): the updates are queued on the batch's stream and the call
+ * returns, so the host admits, polls or fetches while they run.  Errors of the
+ * queued work surface at the next hc_batch_wait or hc_batch_step. */
+int hc_batch_step_async(hc_batch* b, int steps);
+/* Waits for the work queued by hc_batch_step_async (and any admission queued
+ * after it); *n_active (may be NULL) as for hc_batch_step. */
+int hc_batch_wait(hc_batch* b, int* n_active);
 /* Measurement form of hc_batch_step: the same launches, issued directly (not
  * from the captured graph) with CUDA events around every stage kernel on the
  * batch's stream.  Adds the elapsed milliseconds of stage s (all dimensions,
@@ -319,6 +329,11 @@ int hc_batch_step(hc_batch* b, int steps, int* n_active);
 int hc_batch_step_timed(hc_batch* b, int steps, double* stage_ms, int n_stage_ms, double* total_ms);
 /* Lists finished instances not yet reported (at most cap). */
 int hc_batch_poll(hc_batch* b, hc_done* out, int cap, int* n_out);
+/* Lists every occupied slot, finished or not, in slot order (at most cap):
+ * its status so far, tag, updates done and time.  Reports nothing as
+ * finished (hc_batch_poll still does).  No counterpart in the reference: the
+ * batch's progress report. */
+int hc_batch_list(hc_batch* b, hc_done* out, int cap, int* n_out);
 /* Copies a slot's interior state to the host. */
 int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout);
 /* `count` hc_batch_fetch calls in one (slot slots[k] into cons[k], all in

@@ -30,6 +30,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -42,6 +43,8 @@ for p in (PKG, ORACLE_DIR):
 import numpy as np  # noqa: E402
 
 METRIC = "cell-updates/s (FP32 batched)"
+WORKLOAD = ("batched 2D Euler: 512 quadrant Riemann problems, N log-uniform in [64,512] (seed 4), "
+            "plm cons + van Leer, Roe, RK2, CFL .475, gamma 1.4, freeflow")
 UNIT = "cell-updates/s"
 COUNT = 512
 E2E_STEPS = 200          # the configuration's 200 steps per instance
@@ -99,8 +102,7 @@ class ClockSampler:
     def __init__(self, device=0):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/hc_clocks_%d.csv" % os.getpid()
+        self.path = os.path.join(tempfile.gettempdir(), "hc_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:
@@ -144,19 +146,18 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def traffic_from_profiles(cells, stage_bytes_list):
-    """DRAM bytes per stage launch from the committed ncu summary, scaled to this
-    workload by interior cells, or None."""
-    path = os.path.join(ROOT, "profiles", "k_stage_2d_plm_f32_c4.md")
+def traffic_from_profiles(schedule, cells):
+    """DRAM bytes per stage launch of `schedule`, from the committed ncu
+    summary of the batched workload's stage kernel (profiles/traffic.json:
+    dram__bytes_read.sum + dram__bytes_write.sum per interior cell-stage,
+    measured per schedule), scaled by this workload's interior cells; None
+    when that schedule has no capture."""
     try:
-        text = open(path).read()
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f)
+        return float(t["schedules"][str(schedule)]["dram_bytes_per_cell_stage"]) * cells
     except Exception:
         return None
-    import re
-    m = re.search(r"dram_bytes_per_cell_stage:\s*([0-9.eE+-]+)", text)
-    if not m:
-        return None
-    return float(m.group(1)) * cells
 
 
 def cpu_baseline(work, budget_s=12.0, threads=None):
@@ -218,8 +219,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batched 2D Euler quadrants, 512 grids N in [64,512], plm cons + van Leer, Roe, RK2, CFL .475",
-                   "sample": sample},
+        "config": {"workload": WORKLOAD, "cells": sum(a["gridSize"][0] * a["gridSize"][1] for a, _ in work),
+                   "instances": len(work), "parallelism": "host cores (OpenMP)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -237,6 +238,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-requests", type=int, default=1000,
+                    help="requests of the bounded serving run reported in the bench line")
     ap.add_argument("--count", type=int, default=COUNT,
                     help="instances (the configuration has 512; fewer only for profiling a small case)")
     ap.add_argument("--workload", default="c4", choices=["c4", "c1", "c2", "c3", "c5"],
@@ -275,8 +279,10 @@ def main():
     cells = sum(a["gridSize"][0] * a["gridSize"][1] for a, _ in work)
     inputs = [soa5_f32(hc, a, q) for a, q in work]
     b = hc.Batch(ctx, precision="f32", max_slots=len(work), **SCHEME)
+    cells_of = {}
     for k, ((a, _), u) in enumerate(zip(work, inputs)):
-        b.admit(a, u, t_end=math.inf, tag=k, layout="soa5_f32")
+        slot = b.admit(a, u, t_end=math.inf, tag=k, layout="soa5_f32")
+        cells_of[slot] = a["gridSize"][0] * a["gridSize"][1]
     tune_cache = os.path.join(PKG, "_build", "autotune.txt")
     if args.schedule >= 0:
         b.set_schedule(2, args.schedule)
@@ -285,17 +291,35 @@ def main():
     st = b.stats()
     b.step(args.warmup)
 
+    before = {e["slot"]: e for e in b.list()}
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:
         stage_ms, total_ms = b.step_timed(args.steps)
+    after = {e["slot"]: e for e in b.list()}
+    # only the updates every instance actually did are credited: an instance
+    # that went non-finite stops stepping and would otherwise count
+    credited = 0
+    full = 0
+    bad = 0
+    for slot, e in after.items():
+        n = e["steps"] - before[slot]["steps"]
+        credited += cells_of[slot] * n
+        full += n == args.steps and e["status"] == 0
+        bad += e["status"] != 0
     elapsed = total_ms / 1e3
     if dist:
         import torch
-        t = torch.tensor([elapsed], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
-    value = world * cells * args.steps / elapsed
+        c = torch.tensor([float(credited)], dtype=torch.float64, device=dev)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        credited = int(c.item())
+    value = credited / elapsed
+    work_check = {"instances": len(after), "stepped_every_update": full, "status_nonzero": bad,
+                  "credited_cell_updates": credited}
 
     # roofline of the stage kernel: algorithmic bytes per launch / mean launch time
     arrays = stage_arrays(1)
@@ -304,14 +328,13 @@ def main():
     achieved = sum(b_ * args.steps for b_ in stage_bytes) / (sum(stage_ms) / 1e3) / 1e9
     peaks, peak_kind = measured_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = traffic_from_profiles(cells, stage_bytes)
+    traffic = traffic_from_profiles(st["schedule"][1], cells)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "batched 2D Euler: 512 quadrant Riemann problems, N log-uniform in [64,512] (seed 4), "
-                               "plm cons + van Leer, Roe, RK2, CFL .475, gamma 1.4, freeflow",
+        "config": {"workload": WORKLOAD,
                    "cells": cells, "instances": len(work), "l2": "inputs larger than L2 (%.0f MB per state array)" % (
                        cells * FIELDS * BYTES_PER_VALUE / 1e6),
                    "tile": st["tile"][1], "parallelism": "independent grids per GPU" if world > 1 else "1 GPU"},
@@ -322,6 +345,7 @@ def main():
                      "ms_per_launch": sum(stage_ms) / launches},
         "gpu_launches": args.steps * (1 + len(arrays)) + 1,
         "clocks": clk.summary(),
+        "work_check": work_check,
     }
 
     if rank == 0 and not args.no_e2e:
@@ -329,6 +353,8 @@ def main():
     if rank == 0:
         if not args.no_fp64:
             out["fp64"] = fp64_run(hc, ctx, work)
+        if not args.no_serving:
+            out["serving"] = serving_run(hc, ctx, args.serving_requests)
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(work)
         print(json.dumps(out))
@@ -380,7 +406,7 @@ def e2e_run(hc, ctx, work, inputs, cells, schedule, tick=8):
                 b.fetch(ev["slot"], "soa5_f32", out=outs[ev["tag"]])
         t1 = time.perf_counter()
         b.close()
-        return t0, t_admit, t_step, t1, len(evs), calls + 1
+        return t0, t_admit, t_step, t1, evs, calls + 1
 
     try:
         host = np.frombuffer((ctypes.c_char * nbytes).from_address(ptr.value), dtype=np.float32)
@@ -396,14 +422,20 @@ def e2e_run(hc, ctx, work, inputs, cells, schedule, tick=8):
         def run(per_call, many):
             return job(views, outs, per_call, many)
 
-        t0, t_admit, t_step, t1, got, calls = run(tick, True)
+        t0, t_admit, t_step, t1, evs, calls = run(tick, True)
         p0, _, _, p1, _, _ = run(1, True)
         q0, q_admit, q_step, q1, _, _ = run(tick, False)
     finally:
         L.hc_host_free(ptr)
         L.hc_host_free(optr)
     ctl_bytes = STATUS_BYTES_PER_SLOT * len(work)
-    return {"value": cells * E2E_STEPS / (t1 - t0), "unit": UNIT,
+    # credit the updates each instance reports doing
+    credited = sum(work[ev["tag"]][0]["gridSize"][0] * work[ev["tag"]][0]["gridSize"][1] * ev["steps"] for ev in evs)
+    got = len(evs)
+    check = {"instances": len(work), "finished": got,
+             "all_200_updates": sum(1 for ev in evs if ev["steps"] == E2E_STEPS),
+             "status_nonzero": sum(1 for ev in evs if ev["status"] != 0), "credited_cell_updates": credited}
+    return {"value": credited / (t1 - t0), "unit": UNIT, "work_check": check,
             "h2d_bytes_per_step": nbytes / E2E_STEPS, "d2h_bytes_per_step": nbytes / E2E_STEPS + ctl_bytes * calls / E2E_STEPS,
             "steps": E2E_STEPS, "updates_per_call": tick, "instances_fetched": got, "seconds": t1 - t0,
             "seconds_admit": t_admit - t0, "seconds_steps": t_step - t_admit, "seconds_fetch": t1 - t_step,
@@ -420,7 +452,7 @@ def fp64_run(hc, ctx, work):
     """FP64 reference points on the same workload: the plain FP64 form (one
     solver per grid, kernel-for-kernel, host dt read per update) on a sample,
     and the fused FP64 batch on the whole workload."""
-    sample = work[:8]
+    sample = work[::max(1, len(work) // 64)][:64]
     cells = 0
     t = 0.0
     for a, q in sample:
@@ -461,7 +493,9 @@ def fp64_run(hc, ctx, work):
     for k in got["f32"]:
         l1.append(float(np.mean(np.abs(got["f32"][k][:, 0] - got["f64"][k][:, 0]))))
         cells_l1 += got["f32"][k].shape[0]
-    return {"plain_value": plain, "plain_sample": "%d grids x 3 updates" % len(sample),
+    return {"plain_value": plain, "plain_sample": "%d grids (every %dth of the workload, N %d..%d) x 3 updates" % (
+                len(sample), max(1, len(work) // 64), min(a["gridSize"][0] for a, _ in sample),
+                max(a["gridSize"][0] for a, _ in sample)),
             "fused_batched_value": fused, "unit": UNIT,
             "l1_rho_f32_vs_f64": {"max": max(l1), "mean": float(np.mean(l1)),
                                   "sample": "first %d instances (%d cells), %d updates each, FP64 fused batch as the "
@@ -789,30 +823,80 @@ class StatePrefetch:
         self.pool.shutdown(wait=True, cancel_futures=True)
 
 
+SERVE_SCHEME = dict(usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2")
+SERVE_BUDGET = 150 * (1 << 30)
+
+
+def serving_schedules(hc, ctx):
+    """Loads the 1D / 2D / 3D kernels outside any measured run, then tunes the
+    stage-kernel schedules once on a calibration batch of requests drawn from
+    the serving distribution (another seed): the serving batch starts empty,
+    so it has nothing to tune on, and pins these."""
+    import serve
+    warm_reqs = serve.synthetic_stream(24, rate_hz=1e6, seed=11, scale=0.05)
+    wb = hc.Batch(ctx, precision="f32", max_slots=64, hbm_budget=SERVE_BUDGET, **SERVE_SCHEME)
+    serve.Server(wb, steps_per_tick=4, keep_results=False).run(warm_reqs)
+    wb.close()
+    cal = serve.synthetic_stream(48, rate_hz=1e6, seed=13, device_init=True)
+    cb = hc.Batch(ctx, precision="f32", max_slots=64, hbm_budget=SERVE_BUDGET, **SERVE_SCHEME)
+    for r in cal:
+        cb.admit_init(r.args, r.init[0], t_end=math.inf, tag=r.tag, **r.init[1])
+    cb.autotune()
+    schedules = {d: cb.stats()["schedule"][d - 1] for d in (1, 2, 3)}
+    cb.close()
+    return schedules
+
+
+def capacity(reqs, done, wall):
+    """The offered load against what was served: the stream's work (cell
+    updates of the finished requests) over its arrival span, and over the
+    wall time it took to serve."""
+    work = sum(r.steps * int(np.prod(r.args["gridSize"])) for r in done)
+    span = max(r.arrival for r in reqs) if reqs else 0.0
+    offered = work / span if span > 0 else None
+    served = work / wall if wall > 0 else None
+    return {"cell_updates": work, "arrival_span_s": span, "wall_s": wall,
+            "offered_cell_updates_per_s": offered, "served_cell_updates_per_s": served,
+            "offered_over_served": offered / served if offered and served else None,
+            "note": "offered_over_served > 1: the stream brings more work per second than the GPU completes, "
+                    "so requests queue and the latency percentiles are queueing time"}
+
+
+def serving_run(hc, ctx, requests):
+    """A bounded run of the serving configuration's stream (device-built
+    initial states) for the bench line: throughput, completed requests per
+    second, p50 / p99 time-to-solution, and the capacity arithmetic."""
+    import serve
+    schedules = serving_schedules(hc, ctx)
+    reqs = serve.synthetic_stream(requests, rate_hz=200.0, seed=5, device_init=True)
+    b = hc.Batch(ctx, precision="f32", max_slots=1024, hbm_budget=SERVE_BUDGET, **SERVE_SCHEME)
+    for d, v in schedules.items():
+        b.set_schedule(d, v)
+    srv = serve.Server(b, steps_per_tick=8, keep_results=False)
+    t0 = time.perf_counter()
+    done = srv.run(reqs)
+    wall = time.perf_counter() - t0
+    b.close()
+    return {"requests": len(reqs), "finished": len(done), "wall_s": wall,
+            "requests_per_s_completed": len(done) / wall, "arrival_rate_hz": 200.0,
+            "cell_updates_per_s": srv.cell_updates / wall, "latency": serve.latency_summary(done),
+            "statuses_nonzero": sum(1 for r in done if r.status), "ticks": srv.ticks,
+            "host_wait_s": srv.wait_s, "passed_over": srv.passed_over,
+            "capacity": capacity(reqs, done, wall),
+            "schedules": {str(d): v for d, v in schedules.items()},
+            "config": "%d requests of the serving stream (Poisson, mean 200/s, seed 5; 40%% 1D, 45%% 2D, 15%% 3D), "
+                      "plm cons + minmod, RK2, CFL .3, 150 GB budget, FP32" % requests}
+
+
 def run_c5(args):
     """Serving: a Poisson stream (mean 200 requests/s) of 1D / 2D / 3D solves
     through the continuous-batching loop, FP32 bulk, 150 GB HBM budget."""
     import hydrocuda as hc
     import serve
     ctx = hc.Context(0)
-    scheme = dict(usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 2")
-    budget = 150 * (1 << 30)
-    # load the 1D / 2D / 3D kernels outside the measured run
-    warm_reqs = serve.synthetic_stream(24, rate_hz=1e6, seed=11, scale=0.05)
-    wb = hc.Batch(ctx, precision="f32", max_slots=64, hbm_budget=budget, **scheme)
-    serve.Server(wb, steps_per_tick=4, keep_results=False).run(warm_reqs)
-    wb.close()
-
-    # schedules: tuned once on a calibration batch of requests drawn from the
-    # same distribution (another seed), then pinned on the serving batch
-    # (which starts empty, so it has nothing to tune on)
-    cal = serve.synthetic_stream(48, rate_hz=1e6, seed=13, device_init=True)
-    cb = hc.Batch(ctx, precision="f32", max_slots=64, hbm_budget=budget, **scheme)
-    for r in cal:
-        cb.admit_init(r.args, r.init[0], t_end=math.inf, tag=r.tag, **r.init[1])
-    cb.autotune()
-    schedules = {d: cb.stats()["schedule"][d - 1] for d in (1, 2, 3)}
-    cb.close()
+    scheme = SERVE_SCHEME
+    budget = SERVE_BUDGET
+    schedules = serving_schedules(hc, ctx)
 
     device_init = not args.host_states
     reqs = serve.synthetic_stream(args.requests, rate_hz=200.0, seed=5, lazy=True, layout="soa5_f32",
@@ -878,7 +962,8 @@ def run_c5(args):
             "requests_per_s": len(done) / wall, "latency": lat,
             "statuses_nonzero": sum(1 for r in done if r.status),
             "nonfinite_requests": failed,
-            "ticks": srv.ticks, "dims": dims,
+            "ticks": srv.ticks, "dims": dims, "host_wait_s": srv.wait_s, "passed_over": srv.passed_over,
+            "capacity": capacity(reqs, done, wall),
             "initial_states": "built on the device at admission (hc_batch_admit_init)" if device_init else
                               "built on the host by worker threads, uploaded at admission",
             "host_state_wait_s": pre.wait_s if pre else 0.0,

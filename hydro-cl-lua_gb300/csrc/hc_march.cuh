@@ -52,6 +52,37 @@ struct MarchCfg {
 // the y lane sits at frame index kYFrame[g].
 __device__ __forceinline__ constexpr int yFrameOf(int g) { return g == 0 ? 0 : (g == 4 ? 4 : (g == 1 ? 3 : g - 1)); }
 
+// The ghost copies a finished 2D cell (x, y) at padded index idx makes
+// (gridsolver.lua:638-780): periodic wraps, mirror reflects with the normal
+// momentum negated, freeflow repeats the edge cell -- the copies of
+// scatterGhosts, addressed by their offset from idx (a row is px elements).
+__device__ __forceinline__ void marchGhosts(float* out, long long plane, int px, int nx, int ny, const int* bc, int x,
+                                            int y, long long idx, const float* u) {
+    auto put = [&](long long off, int negf) {
+#pragma unroll
+        for (int f = 0; f < 5; ++f) out[f * plane + idx + off] = f == negf ? -1.f * u[f] : u[f];
+    };
+    if (x < 2 || x >= nx - 2) {
+        int const lo = bc[0], hi = bc[1];
+        if (lo == HC_BOUNDARY_PERIODIC && x >= nx - 2) put(-nx, -1);
+        if (lo == HC_BOUNDARY_MIRROR && x <= 1) put(-1 - 2 * x, 1);
+        if (lo == HC_BOUNDARY_FREEFLOW && x == 0) { put(-1, -1); put(-2, -1); }
+        if (hi == HC_BOUNDARY_PERIODIC && x <= 1) put(nx, -1);
+        if (hi == HC_BOUNDARY_MIRROR && x >= nx - 2) put(2 * nx - 1 - 2 * x, 1);
+        if (hi == HC_BOUNDARY_FREEFLOW && x == nx - 1) { put(1, -1); put(2, -1); }
+    }
+    if (y < 2 || y >= ny - 2) {
+        int const lo = bc[2], hi = bc[3];
+        long long const r = px;
+        if (lo == HC_BOUNDARY_PERIODIC && y >= ny - 2) put(-ny * r, -1);
+        if (lo == HC_BOUNDARY_MIRROR && y <= 1) put((-1 - 2 * y) * r, 2);
+        if (lo == HC_BOUNDARY_FREEFLOW && y == 0) { put(-r, -1); put(-2 * r, -1); }
+        if (hi == HC_BOUNDARY_PERIODIC && y <= 1) put(ny * r, -1);
+        if (hi == HC_BOUNDARY_MIRROR && y >= ny - 2) put((2 * ny - 1 - 2 * y) * r, 2);
+        if (hi == HC_BOUNDARY_FREEFLOW && y == ny - 1) { put(r, -1); put(2 * r, -1); }
+    }
+}
+
 template <int NW, int H, int C, int NB, int SLOPE, int OCC>
 __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__ StageArgs a, int slopeLim, int fluxLim) {
     using Cfg = MarchCfg<NW, C, NB>;
@@ -143,6 +174,29 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
 
         float* const out = reinterpret_cast<float*>(I.buf[slotBuf(st.out_buf, rot, a.rot_buf)]);
         float* const dstore = st.store_deriv >= 0 ? reinterpret_cast<float*>(I.dbuf[st.store_deriv]) : nullptr;
+        // the first Runge-Kutta state the epilogue reads from global memory
+        // (not the staged input): read one step ahead into registers, so its
+        // latency overlaps a step's flux arithmetic
+        int a0 = -1;
+        const float* a0src = nullptr;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            if (m >= st.n_alpha) break;
+            int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
+            if (b != inBuf && a0 < 0) {
+                a0 = m;
+                a0src = reinterpret_cast<const float*>(I.buf[b]);
+            }
+        }
+        // padded index of cell (x, y0); row r adds r * px
+        long long const idx0 = padIndex<2>(geo, x, y0, 0);
+        float pre[5];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) pre[f] = 0.f;
+        if (a0 >= 0 && inCols) {
+#pragma unroll
+            for (int f = 0; f < 5; ++f) pre[f] = a0src[f * geo.plane + idx0];
+        }
 
         float dtmin = fast::M<float>::inf();
         bool bad = false;
@@ -237,10 +291,13 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                 if (fin) {
                     // cell (x, r-1): u = sum alpha_k u^(k) + sum (beta_k dt) L(u^(k)) + (beta_cur dt) deriv
                     int const yc = y0 - 3 + ir;
-                    long long const idx = padIndex<2>(geo, x, yc, 0);
+                    long long const idx = idx0 + (long long)(ir - 3) * geo.px;
                     auto ldAlpha = [&](int m, float* v) {
                         int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
-                        if (b == inBuf) {
+                        if (m == a0) {
+#pragma unroll
+                            for (int f = 0; f < 5; ++f) v[f] = pre[f];
+                        } else if (b == inBuf) {
 #pragma unroll
                             for (int f = 0; f < 5; ++f) v[f] = at(f, ir - 1, col);
                         } else {
@@ -264,6 +321,11 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
 #pragma unroll
                         for (int f = 0; f < 5; ++f) u[f] = lanes::fma(lanes::sub(w[f], p[f]), K.calpha[m], u[f]);
                     }
+                    // the next step's cell
+                    if (a0 >= 0 && yc + 1 < y0 + rows) {
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) pre[f] = a0src[f * geo.plane + idx + geo.px];
+                    }
 #pragma unroll
                     for (int m = 0; m < 4; ++m) {
                         if (m >= st.n_beta) break;
@@ -284,7 +346,7 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                     }
                     // after constrainU a non-finite momentum shows in ETotal
                     bad |= !fast::M<float>::finite_(u[0] + u[4]);
-                    scatterGhosts<float, 2>(geo, out, x, yc, 0, u);
+                    marchGhosts(out, geo.plane, geo.px, nx, ny, geo.bc, x, yc, idx, u);
                     if (st.last) dtmin = fast::tmin(dtmin, lanes::dtCell<float, 2>(u, le, K.gdx));
                 }
             }

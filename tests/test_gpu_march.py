@@ -95,6 +95,17 @@ def test_march_equals_tile_boundaries(hc, ctx, bi):
         np.testing.assert_array_equal(x, y)
 
 
+@pytest.mark.parametrize("schedule", [17, 18])
+def test_march_occupancy_variants(hc, ctx, schedule):
+    """The same kernel compiled for 3 and 2 CTAs per SM."""
+    probs = [_quad(hc, nx, ny, 90 + k) for k, (nx, ny) in enumerate([(61, 63), (150, 129)])]
+    scheme = dict(usePLM="plm cons", slopeLimiter="van Leer (abs)", integrator="Runge-Kutta 2")
+    a = _run(hc, ctx, probs, scheme, schedule, 6)
+    b = _run(hc, ctx, probs, scheme, TILE, 6)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_march_against_oracle(hc, ctx):
     """FP32 marching kernel against the FP64 oracle: density L1 <= 1e-5 after 20 updates."""
     a, u = _quad(hc, 123, 77, 5)

@@ -189,11 +189,11 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
             }
         }
         // padded index of cell (x, y0); row r adds r * px
-        long long const idx0 = padIndex<2>(geo, x, y0, 0);
+        long long const idx0 = padIndex<2>(geo, xc, y0, 0);
         float pre[5];
 #pragma unroll
         for (int f = 0; f < 5; ++f) pre[f] = 0.f;
-        if (a0 >= 0 && inCols) {
+        if (a0 >= 0) {
 #pragma unroll
             for (int f = 0; f < 5; ++f) pre[f] = a0src[f * geo.plane + idx0];
         }
@@ -216,6 +216,9 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
 
         // step ir: r = y0 - 2 + ir, slopes of (x, r), the x face flux of row r,
         // the y face flux below (x, r), cell (x, r-1) finished from ir = 3 on
+        // (every lane evaluates it; only the strip's own cells are stored)
+        bool const edgeX = x0 < 2 || x0 + kStripW > nx - 2;   // the strip holds cells with x ghost copies
+        float const arx = K.area[0], ary = K.area[1];
 #pragma unroll 1
         for (int ir = 1; ir <= rows + 2; ++ir) {
             if (timedOut) break;
@@ -228,14 +231,18 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
             }
             while (ready <= (ir + 1) / C) waitChunk();
             if (timedOut) break;
+            // the lane's column in box rows ir - 1, ir, ir + 1
+            const float* const rm = wb + ((ir - 1) / C % NB) * Cfg::BUFF + ((ir - 1) % C) * kMarchBW + col;
+            const float* const r0 = wb + (ir / C % NB) * Cfg::BUFF + (ir % C) * kMarchBW + col;
+            const float* const rp = wb + ((ir + 1) / C % NB) * Cfg::BUFF + ((ir + 1) % C) * kMarchBW + col;
             // x and y half slopes of (x, r): L = U - h, R = U + h
             float2 L[5], R[5];
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
-                float const u0 = at(f, ir, col);
+                float const u0 = r0[f * C * kMarchBW];
                 float2 const c = make_float2(u0, u0);
-                float2 const dL = lanes::sub(c, make_float2(at(f, ir, col - 1), at(f, ir - 1, col)));
-                float2 const dR = lanes::sub(make_float2(at(f, ir, col + 1), at(f, ir + 1, col)), c);
+                float2 const dL = lanes::sub(c, make_float2(r0[f * C * kMarchBW - 1], rm[f * C * kMarchBW]));
+                float2 const dR = lanes::sub(make_float2(r0[f * C * kMarchBW + 1], rp[f * C * kMarchBW]), c);
                 float2 const h = lanes::halfSlope<SLOPE>(dL, dR, slim);
                 L[f] = lanes::sub(c, h);
                 R[f] = lanes::add(c, h);
@@ -275,20 +282,20 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                 }
                 if (zeroX) for (int j = 0; j < 5; ++j) F[j].x = 0.f;
                 if (zeroY) for (int j = 0; j < 5; ++j) F[j].y = 0.f;
-                bool const fin = ir >= 3 && inCols;
+                // calcDerivFromFlux: x difference of (x, r) (its right face flux
+                // by shuffle), then the y difference of (x, r-1) added to its x
+                // difference, each fma(FL - FR, area, deriv) rounded as written
                 float deriv[5];
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
                     float const fx = F[f].x;
                     float const fy = F[yFrameOf(f)].y;
                     float const fxr = __shfl_down_sync(FULL, fx, 1);
-                    float2 const d = lanes::sub(make_float2(fx, Fyp[f]), make_float2(fxr, fy));
-                    float2 const D = lanes::fma(d, area, make_float2(0.f, Dxp[f]));
-                    deriv[f] = skipY ? Dxp[f] : D.y;
-                    Dxp[f] = skipX ? 0.f : D.x;
+                    deriv[f] = skipY ? Dxp[f] : __fmaf_rn(__fsub_rn(Fyp[f], fy), ary, Dxp[f]);
+                    Dxp[f] = skipX ? 0.f : __fmaf_rn(__fsub_rn(fx, fxr), arx, 0.f);
                     Fyp[f] = fy;
                 }
-                if (fin) {
+                if (ir >= 3) {
                     // cell (x, r-1): u = sum alpha_k u^(k) + sum (beta_k dt) L(u^(k)) + (beta_cur dt) deriv
                     int const yc = y0 - 3 + ir;
                     long long const idx = idx0 + (long long)(ir - 3) * geo.px;
@@ -299,7 +306,7 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                             for (int f = 0; f < 5; ++f) v[f] = pre[f];
                         } else if (b == inBuf) {
 #pragma unroll
-                            for (int f = 0; f < 5; ++f) v[f] = at(f, ir - 1, col);
+                            for (int f = 0; f < 5; ++f) v[f] = rm[f * C * kMarchBW];
                         } else {
                             const float* const src = reinterpret_cast<const float*>(I.buf[b]);
 #pragma unroll
@@ -338,16 +345,22 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                         for (int f = 0; f < 5; ++f) u[f] = lanes::fma(deriv[f], cbcur, u[f]);
                     }
                     lanes::constrain<float>(u, le, K.invg1);
+                    if (inCols) {
 #pragma unroll
-                    for (int f = 0; f < 5; ++f) out[f * geo.plane + idx] = u[f];
-                    if (dstore) {
+                        for (int f = 0; f < 5; ++f) out[f * geo.plane + idx] = u[f];
+                        if (dstore) {
 #pragma unroll
-                        for (int f = 0; f < 5; ++f) dstore[f * geo.plane + idx] = deriv[f];
+                            for (int f = 0; f < 5; ++f) dstore[f * geo.plane + idx] = deriv[f];
+                        }
                     }
                     // after constrainU a non-finite momentum shows in ETotal
-                    bad |= !fast::M<float>::finite_(u[0] + u[4]);
-                    marchGhosts(out, geo.plane, geo.px, nx, ny, geo.bc, x, yc, idx, u);
-                    if (st.last) dtmin = fast::tmin(dtmin, lanes::dtCell<float, 2>(u, le, K.gdx));
+                    bad |= inCols && !fast::M<float>::finite_(u[0] + u[4]);
+                    if (edgeX || yc < 2 || yc >= ny - 2)
+                        if (inCols) marchGhosts(out, geo.plane, geo.px, nx, ny, geo.bc, x, yc, idx, u);
+                    if (st.last) {
+                        float const dtc = lanes::dtCell<float, 2>(u, le, K.gdx);
+                        if (inCols) dtmin = fast::tmin(dtmin, dtc);
+                    }
                 }
             }
 #pragma unroll

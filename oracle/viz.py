@@ -329,9 +329,11 @@ def volume(tex, n, mins, maxs, width, height, vmin, vmax, eye, fov_y=45., palett
     rgb += (ra * a)[..., None] * c[..., :3]
     ra = ra * (f32(1) - a)
     dd = [start[k] - e[k] for k in range(3)]
-    with np.errstate(all="ignore"):   # rays that miss the box have no step (masked below)
+    with np.errstate(all="ignore"):
         inv = f32(1) / (np.sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]) * f32(max_iter))
-        step = [dd[k] * inv for k in range(3)]
+        # a ray that misses the box has no step (0/0): it stays where it is, at
+        # finite coordinates, and is masked out of the composite below
+        step = [np.where(hit, dd[k] * inv, f32(0)) for k in range(3)]
     alive = hit.copy()
     for i in range(2, max_iter + 1):
         p = [p[k] + step[k] for k in range(3)]

@@ -40,3 +40,12 @@ def c4_quadrant(n, **kw):
              cfl=.475, eqnArgs={"heatCapacityRatio": 1.4})
     a.update(kw)
     return a
+
+
+def c4_workload(count=512, seed=4):
+    """The batched quadrant workload as the benchmark builds it: `count` grids
+    with N log-uniform in [64, 512] (SplitMix64 seed 4), instance i's quadrant
+    states from SplitMix64(100000 + i).  Returns [(args, quadrants)]."""
+    import hydrocuda as hc
+    sizes = hc.batched_quadrant_sizes(count, seed)
+    return [(c4_quadrant(n), hc.random_quadrants(hc.SplitMix64(100000 + i))) for i, n in enumerate(sizes)]

@@ -141,7 +141,7 @@ def test_volume(hc, ctx, isobars, lighting):
                    use_isobars=isobars, use_lighting=lighting)
     want = viz.volume(tex, s.gridSize, args["mins"], args["maxs"], 40, 32, .1, 1., eye, max_iter=48,
                       use_isobars=isobars, use_lighting=lighting)
-    _close_images(got, want, frac=.99, tol=3)
+    _close_images(got, want)
     assert got[..., 3].max() > 0
 
 

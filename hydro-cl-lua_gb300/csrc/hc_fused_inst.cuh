@@ -83,15 +83,26 @@ void add_march2(std::vector<StageLauncher>& v) {
     sl.box[2] = 1;
     sl.march = 1;
     sl.smem = Cfg::SMEM;
+    // one kernel per epilogue form; the stage's plan picks it at launch
     sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
-        k_march2<NW, H, C, NB, SLOPE, OCC><<<grid, NW * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+        switch (marchEpi(a.st)) {
+        case 1: k_march2<NW, H, C, NB, SLOPE, OCC, 1><<<grid, NW * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim); break;
+        case 2: k_march2<NW, H, C, NB, SLOPE, OCC, 2><<<grid, NW * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim); break;
+        case 3: k_march2<NW, H, C, NB, SLOPE, OCC, 3><<<grid, NW * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim); break;
+        default: k_march2<NW, H, C, NB, SLOPE, OCC, 0><<<grid, NW * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+        }
     };
     sl.occupancy = []() -> int {
-        auto k = k_march2<NW, H, C, NB, SLOPE, OCC>;
-        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
-        int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NW * 32, Cfg::SMEM) != cudaSuccess) return -1;
-        return n;
+        void (*ks[4])(StageArgs, int, int) = {k_march2<NW, H, C, NB, SLOPE, OCC, 0>, k_march2<NW, H, C, NB, SLOPE, OCC, 1>,
+                                              k_march2<NW, H, C, NB, SLOPE, OCC, 2>, k_march2<NW, H, C, NB, SLOPE, OCC, 3>};
+        int occ = 1 << 30;
+        for (auto k : ks) {
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
+            int n = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NW * 32, Cfg::SMEM) != cudaSuccess) return -1;
+            occ = n < occ ? n : occ;
+        }
+        return occ;
     };
     v.push_back(sl);
 }

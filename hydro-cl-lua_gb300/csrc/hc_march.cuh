@@ -48,6 +48,20 @@ struct MarchCfg {
     static constexpr unsigned BYTES = (unsigned)(BUFF * 4);
 };
 
+// The epilogue forms the launcher compiles (EPI): 0 reads the stage's
+// structure at run time; the others have it fixed -- no stored derivatives
+// and no beta terms, a current-derivative term, and the alpha terms
+//   1: the staged input alone (forward Euler, the first stage of RK2 / RK3-TVD)
+//   2: one state from global memory (the midpoint RK2's second stage)
+//   3: one state from global memory, then the staged input (the later stages
+//      of RK2-TVD and RK3-TVD)
+inline int marchEpi(const StageDev& s) {
+    if (s.n_beta != 0 || s.store_deriv >= 0 || s.beta_cur == 0.) return 0;
+    if (s.n_alpha == 1) return s.alpha_buf[0] == s.in_buf ? 1 : 2;
+    if (s.n_alpha == 2 && s.alpha_buf[0] != s.in_buf && s.alpha_buf[1] == s.in_buf) return 3;
+    return 0;
+}
+
 // The y axis' interface frame takes (rho, m.y, m.z, m.x, E): global field g of
 // the y lane sits at frame index kYFrame[g].
 __device__ __forceinline__ constexpr int yFrameOf(int g) { return g == 0 ? 0 : (g == 4 ? 4 : (g == 1 ? 3 : g - 1)); }
@@ -83,7 +97,7 @@ __device__ __forceinline__ void marchGhosts(float* out, long long plane, int px,
     }
 }
 
-template <int NW, int H, int C, int NB, int SLOPE, int OCC>
+template <int NW, int H, int C, int NB, int SLOPE, int OCC, int EPI>
 __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__ StageArgs a, int slopeLim, int fluxLim) {
     using Cfg = MarchCfg<NW, C, NB>;
     (void)fluxLim;
@@ -299,6 +313,8 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                     // cell (x, r-1): u = sum alpha_k u^(k) + sum (beta_k dt) L(u^(k)) + (beta_cur dt) deriv
                     int const yc = y0 - 3 + ir;
                     long long const idx = idx0 + (long long)(ir - 3) * geo.px;
+                    float u[5];
+                    if constexpr (EPI == 0) {
                     auto ldAlpha = [&](int m, float* v) {
                         int const b = slotBuf(st.alpha_buf[m], rot, a.rot_buf);
                         if (m == a0) {
@@ -314,7 +330,7 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                         }
                     };
                     int const last = st.n_alpha - 1;
-                    float p[5], u[5];
+                    float p[5];
 #pragma unroll
                     for (int m = 0; m < 4; ++m)
                         if (m == last) ldAlpha(m, p);
@@ -344,11 +360,37 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
 #pragma unroll
                         for (int f = 0; f < 5; ++f) u[f] = lanes::fma(deriv[f], cbcur, u[f]);
                     }
+                    } else {
+                        // the stage's structure is fixed at compile time (the
+                        // launcher picks the kernel): the same operations as
+                        // above in the same order, without the run-time choices
+                        if constexpr (EPI == 1) {
+#pragma unroll
+                            for (int f = 0; f < 5; ++f) u[f] = rm[f * C * kMarchBW];
+                        } else if constexpr (EPI == 2) {
+#pragma unroll
+                            for (int f = 0; f < 5; ++f) u[f] = pre[f];
+                        } else {
+#pragma unroll
+                            for (int f = 0; f < 5; ++f) {
+                                float const pb = rm[f * C * kMarchBW];
+                                u[f] = lanes::fma(lanes::sub(pre[f], pb), K.calpha[0], pb);
+                            }
+                        }
+                        if constexpr (EPI != 1) {
+                            if (yc + 1 < y0 + rows) {
+#pragma unroll
+                                for (int f = 0; f < 5; ++f) pre[f] = a0src[f * geo.plane + idx + geo.px];
+                            }
+                        }
+#pragma unroll
+                        for (int f = 0; f < 5; ++f) u[f] = lanes::fma(deriv[f], cbcur, u[f]);
+                    }
                     lanes::constrain<float>(u, le, K.invg1);
                     if (inCols) {
 #pragma unroll
                         for (int f = 0; f < 5; ++f) out[f * geo.plane + idx] = u[f];
-                        if (dstore) {
+                        if (EPI == 0 && dstore) {
 #pragma unroll
                             for (int f = 0; f < 5; ++f) dstore[f * geo.plane + idx] = deriv[f];
                         }

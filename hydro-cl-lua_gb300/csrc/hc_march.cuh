@@ -235,7 +235,6 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
         float const arx = K.area[0], ary = K.area[1];
 #pragma unroll 1
         for (int ir = 1; ir <= rows + 2; ++ir) {
-            if (timedOut) break;
             // step ir reads box rows ir - 1 .. ir + 1: chunk (ir - 1) / C - 1 is
             // no longer read, refill its buffer
             if ((ir - 1) % C == 0 && ir - 1 >= C) {
@@ -243,8 +242,11 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                 __syncwarp();
                 if (lane == 0 && k < nchunks) issue(k);
             }
-            while (ready <= (ir + 1) / C) waitChunk();
-            if (timedOut) break;
+            if (ready <= (ir + 1) / C) {
+                do waitChunk();
+                while (ready <= (ir + 1) / C);
+                if (timedOut) break;
+            }
             // the lane's column in box rows ir - 1, ir, ir + 1
             const float* const rm = wb + ((ir - 1) / C % NB) * Cfg::BUFF + ((ir - 1) % C) * kMarchBW + col;
             const float* const r0 = wb + (ir / C % NB) * Cfg::BUFF + (ir % C) * kMarchBW + col;
@@ -382,6 +384,13 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
 #pragma unroll
                                 for (int f = 0; f < 5; ++f) pre[f] = a0src[f * geo.plane + idx + geo.px];
                             }
+                            // and into L2 eight rows ahead (the last row of the
+                            // segment repeated near its end)
+                            int const ahead = yc + 8 < y0 + rows ? 8 : y0 + rows - 1 - yc;
+                            const float* const pf = a0src + idx + (long long)ahead * geo.px;
+#pragma unroll
+                            for (int f = 0; f < 5; ++f)
+                                asm volatile("prefetch.global.L2 [%0];" ::"l"(pf + f * geo.plane));
                         }
 #pragma unroll
                         for (int f = 0; f < 5; ++f) u[f] = lanes::fma(deriv[f], cbcur, u[f]);

@@ -684,7 +684,9 @@ __global__ void k_minReduceScaled(const double* in, long long n, double cfl, dou
 __global__ void k_writeScalar(double v, double* out) { *out = v; }
 
 // Device address of g_noalloc_partial per device, looked up once per device
-// (with that device current) on its first call.
+// (with that device current) on its first call and kept for the life of the
+// process: after a cudaDeviceReset the module may load elsewhere, so the entry
+// point is not for use after one (see the header).
 constexpr int kMaxDevices = 64;
 double* g_noalloc_ptr[kMaxDevices] = {nullptr};
 std::mutex g_noalloc_mutex;
@@ -711,33 +713,45 @@ int noalloc_scratch(double** out) {
 extern "C" int hc_calc_dt_noalloc(const hc_solver_desc* d, const double* state, double* dt_out, void* stream) {
     using namespace hc;
     if (!d || !state || !dt_out) return fail(HC_ERR_INVALID, "NULL argument");
+    // the fields this call reads, with the rules hc_solver_create applies
     if (d->dim < 1 || d->dim > 3) return fail(HC_ERR_INVALID, "dim must be 1, 2 or 3");
+    for (int k = 0; k < d->dim; ++k) {
+        if (d->n[k] < 2) return fail(HC_ERR_INVALID, "each active axis needs at least 2 cells");
+        if (d->n[k] > HC_NOALLOC_MAX_CELLS)
+            return fail(HC_ERR_INVALID, "hc_calc_dt_noalloc: the grid has more than HC_NOALLOC_MAX_CELLS cells");
+        if (!(d->maxs[k] > d->mins[k])) return fail(HC_ERR_INVALID, "maxs must exceed mins");
+    }
+    if (!(d->gamma > 1.)) return fail(HC_ERR_INVALID, "gamma must exceed 1");
+    if (!(d->cfl > 0.) && !(d->fixed_dt > 0.)) return fail(HC_ERR_INVALID, "cfl or fixed_dt must be positive");
     PlainParams p;
     std::memset(&p, 0, sizeof(p));
     p.dim = d->dim;
+    long long cells = 1;
     for (int k = 0; k < 3; ++k) {
         int const n = k < d->dim ? d->n[k] : 1;
-        if (n < 1) return fail(HC_ERR_INVALID, "gridSize must be positive");
         p.gs[k] = k < d->dim ? n + 2 * kGhost : 1;
         p.grid_dx[k] = (d->maxs[k] - d->mins[k]) / (double)n;
+        cells *= p.gs[k];
+        if (cells > HC_NOALLOC_MAX_CELLS)
+            return fail(HC_ERR_INVALID, "hc_calc_dt_noalloc: the grid (ghosts included) has more than HC_NOALLOC_MAX_CELLS cells");
     }
     p.stepsize[0] = 1;
     p.stepsize[1] = p.gs[0];
     p.stepsize[2] = p.gs[0] * p.gs[1];
-    p.numCells = (long long)p.gs[0] * p.gs[1] * p.gs[2];
-    if (p.numCells > HC_NOALLOC_MAX_CELLS)
-        return fail(HC_ERR_INVALID, "hc_calc_dt_noalloc: the grid (ghosts included) has more than HC_NOALLOC_MAX_CELLS cells");
+    p.numCells = cells;
     p.gamma = d->gamma;
     p.rhoMin = d->rho_min;
     p.PMin = d->p_min;
+    // the per-device set-up (the scratch array's address) happens on every
+    // first call on a device, whatever the descriptor asks for
+    double* scratch = nullptr;
+    HC_CHECK(noalloc_scratch(&scratch));
     cudaStream_t const s = static_cast<cudaStream_t>(stream);
     if (d->fixed_dt > 0) {
         k_writeScalar<<<1, 1, 0, s>>>(d->fixed_dt, dt_out);
         HC_CUDA(cudaGetLastError());
         return HC_OK;
     }
-    double* scratch = nullptr;
-    HC_CHECK(noalloc_scratch(&scratch));
     long long const blocks = (p.numCells + kThreads - 1) / kThreads;
     k_calcDT<<<(unsigned)blocks, kThreads, 0, s>>>(p, reinterpret_cast<const Cons*>(state), scratch);
     k_minReduceScaled<<<1, 1024, 0, s>>>(scratch, blocks, d->cfl, dt_out);

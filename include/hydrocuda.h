@@ -446,25 +446,28 @@ int hc_solver_render(hc_solver* s, const hc_render* r, unsigned char* rgba);
 
 /* ---- calcDT without allocation ---------------------------------------------
  *
- * No counterpart in the reference.  For callers that cannot allocate device
- * memory when they need a time step -- code recording a CUDA graph (cudaMalloc
- * is refused during stream capture), code whose device memory is owned by an
- * external allocator, real-time loops that cannot take cudaMalloc's implicit
- * synchronisation.  The same calcDT as hc_solver_calc_dt on the plain FP64
- * form: `state` is that form's UBuf in device memory (cons_t as 6 doubles per
- * cell, x-fastest, numGhost = 2 ghost layers on each active axis); cfl * min
- * (or fixed_dt when > 0) is written to the double at `dt_out` in device memory,
- * on `stream` (a cudaStream_t; NULL = the legacy default stream).  Only the
- * descriptor's dim, n, mins, maxs, gamma, rho_min, p_min, cfl and fixed_dt are
- * read.  It allocates nothing: the reduction's block minima go to a fixed
- * array inside the library (512 KiB, held on every device that loads the
- * library until the process exits), which caps the grid at
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory when they need a time step: code whose device memory belongs to an
+ * outside allocator (a framework's caching allocator, a fixed arena handed to
+ * the library), and loops that cannot take cudaMalloc's implicit device-wide
+ * synchronisation or its unbounded time.  The same calcDT as
+ * hc_solver_calc_dt on the plain FP64 form: `state` is that form's UBuf in
+ * device memory (cons_t as 6 doubles per cell, x-fastest, numGhost = 2 ghost
+ * layers on each active axis); cfl * min (or fixed_dt when > 0) is written to
+ * the double at `dt_out` in device memory, on `stream` (a cudaStream_t; NULL =
+ * the legacy default stream).  Only the descriptor's dim, n, mins, maxs, gamma,
+ * rho_min, p_min, cfl and fixed_dt are read, and they are checked as
+ * hc_solver_create checks them.  It allocates nothing: the reduction's block
+ * minima go to a fixed array inside the library (512 KiB, held on every device
+ * that loads the library until the process exits), which caps the grid at
  * HC_NOALLOC_MAX_CELLS cells including ghosts; larger grids return
  * HC_ERR_INVALID.  The first call on a device looks up that array's address
- * (with the device current), so make it before any stream capture.  Every
- * call shares the array: calls whose kernels may overlap on the GPU (other
- * streams, other host threads) race and must be serialised by the caller.
- * Nothing in the array needs clearing between calls. */
+ * (with the device current), so make it before any stream capture; the
+ * address is kept for the process's life, so the entry point is not for use
+ * after a cudaDeviceReset.  Every call shares the array: calls whose kernels
+ * may overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Nothing in the array needs clearing between
+ * calls. */
 #define HC_NOALLOC_MAX_CELLS (1 << 24)
 int hc_calc_dt_noalloc(const hc_solver_desc* desc, const double* state, double* dt_out, void* stream);
 

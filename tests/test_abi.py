@@ -124,19 +124,28 @@ def test_init_defaults_without_a_device():
     assert list(q.p) == [1, 2, 3, 4] * 4
 
 
-def test_integration_c_examples_compile(tmp_path):
-    """The C snippets of INTEGRATION.md compile against the header, in order in
-    one function (the batch snippet uses the first one's context)."""
+def test_integration_c_example_compiles():
+    """The C usage the integration notes show (tests/fixtures/integration_example.c)
+    compiles against the header with every warning an error."""
     import subprocess
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```c\n(.*?)```", text, flags=re.S)
-    assert len(blocks) >= 2
-    body = "\n".join(l for b in blocks for l in b.splitlines() if not l.startswith("#include"))
-    src = tmp_path / "snippets.c"
-    src.write_text("\n".join([
-        "#include <stdio.h>", "#include <stddef.h>", '#include "hydrocuda.h"',
-        "void example(double* cons_aos6, int count, const hc_solver_desc* descs, const void* const* states,",
-        "             const long long* max_steps, void** results) {",
-        body, "}"]))
+    src = os.path.join(ROOT, "tests", "fixtures", "integration_example.c")
     subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-Wno-unused-variable", "-fsyntax-only",
-                           "-I", os.path.join(ROOT, "include"), str(src)])
+                           "-I", os.path.join(ROOT, "include"), src])
+
+
+def test_noalloc_rejects_bad_descriptors_before_the_device():
+    """hc_calc_dt_noalloc checks the fields it reads as solver creation does,
+    and sizes before adding ghosts, without touching a device."""
+    import hydrocuda
+    L = hydrocuda.load_library()
+    base = dict(dim=2, gridSize=[8, 8], mins=[-1, -1, -1], maxs=[1, 1, 1], boundary="freeflow", cfl=.5)
+    buf = ctypes.c_void_p(16)      # never dereferenced: every case fails first
+    bad = []
+    d = hydrocuda.make_desc(base); d.n[0] = 1; bad.append(d)                       # fewer than 2 cells
+    d = hydrocuda.make_desc(base); d.maxs[1] = d.mins[1]; bad.append(d)           # empty extent
+    d = hydrocuda.make_desc(base); d.gamma = 1.0; bad.append(d)                   # gamma not above 1
+    d = hydrocuda.make_desc(base); d.cfl = 0.0; d.fixed_dt = 0.0; bad.append(d)   # no dt rule
+    d = hydrocuda.make_desc(base); d.n[0] = 2 ** 31 - 2; bad.append(d)           # overflows with ghosts
+    d = hydrocuda.make_desc(base); d.n[0] = 4096; d.n[1] = 4096; bad.append(d)    # beyond the scratch
+    for d in bad:
+        assert L.hc_calc_dt_noalloc(ctypes.byref(d), buf, buf, None) == -1

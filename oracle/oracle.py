@@ -13,6 +13,7 @@ the eigen-basis identities the reference uses as diagnostics
 """
 import ctypes
 import os
+import platform
 import subprocess
 
 import numpy as np
@@ -20,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
+LIB_CONTRACT_PATH = os.path.join(BUILD_DIR, "liboracle_contract.so")
 SRC = os.path.join(HERE, "hydro_oracle.cpp")
 
 # Names in the order of the reference's limiter table (hydro/app.lua:614-635).
@@ -44,17 +46,25 @@ BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3, "linear": 4,
 RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2, "plm prim": 3, "plm athena": 4}
 
 
-def build(force=False):
-    """Compile the oracle with g++ (no FMA contraction, OpenMP)."""
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
-        return LIB_PATH
+def build(force=False, contract=False):
+    """Compile the oracle with g++ (OpenMP).  The default build forbids FMA
+    contraction (-ffp-contract=off): its order of operations is the
+    reference's, term by term.  contract=True builds a second library that lets
+    the compiler fuse multiply-adds (-ffp-contract=fast, with FMA instructions
+    enabled on x86-64), as an OpenCL compiler may under FP_CONTRACT ON: the
+    tests use it to bound how far such a build of the reference can drift from
+    the contraction-free reading."""
+    path = LIB_CONTRACT_PATH if contract else LIB_PATH
+    if not force and os.path.exists(path) and os.path.getmtime(path) >= os.path.getmtime(SRC):
+        return path
     os.makedirs(BUILD_DIR, exist_ok=True)
-    tmp = LIB_PATH + ".tmp%d" % os.getpid()
-    cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
-           "-shared", "-fPIC", SRC, "-o", tmp]
+    tmp = path + ".tmp%d" % os.getpid()
+    fp = ["-ffp-contract=fast"] + (["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []) if contract \
+        else ["-ffp-contract=off"]
+    cmd = ["g++", "-O3", "-std=c++17"] + fp + ["-fno-fast-math", "-fopenmp", "-shared", "-fPIC", SRC, "-o", tmp]
     subprocess.check_call(cmd)
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, path)
+    return path
 
 
 class OrDesc(ctypes.Structure):
@@ -81,13 +91,12 @@ class OrDesc(ctypes.Structure):
 FLUXES = ["roe", "hll", "rusanov", "euler-hllc"]
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = build()
+def lib(contract=False):
+    if contract not in _libs:
+        path = build(contract=contract)
         L = ctypes.CDLL(path)
         vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
         L.or_create.restype = vp
@@ -118,8 +127,8 @@ def lib():
         L.or_limiter.argtypes = [ip, ctypes.c_double]
         L.or_num_threads.restype = ctypes.c_int
         L.or_set_plm_athena_recorded_edges.argtypes = [ip]
-        _lib = L
-    return _lib
+        _libs[contract] = L
+    return _libs[contract]
 
 
 def _ptr(a):
@@ -164,10 +173,10 @@ def make_desc(cfg):
 class OracleSolver:
     """The oracle behind the reference's solver-args vocabulary."""
 
-    def __init__(self, cfg):
+    def __init__(self, cfg, contract=False):
         self.cfg = dict(cfg)
         self.desc = make_desc(cfg)
-        self.L = lib()
+        self.L = lib(contract)
         self.h = self.L.or_create(ctypes.byref(self.desc))
         if not self.h:
             raise ValueError("oracle rejected the configuration")

@@ -82,6 +82,28 @@ function CudaFVSolver:init(args)
 	self.hcNeedsUpload = true
 end
 
+-- The update's OpenCL kernels (calcLR, calcFlux, calcDerivFromFlux) are
+-- replaced by libhydrocuda, so their modules leave the solver program: they
+-- are neither generated nor compiled (SolverBase:refreshSolverProgram,
+-- solverbase.lua:1670-1735, builds the program from solverModulesEnabled;
+-- fvsolver.lua:41,49 and gridsolver.lua:351 add these three).  The rest --
+-- display variables, boundary, constrainU, calcDT -- stays for the OpenCL
+-- side's own uses (display, GUI, the boundary fill before the first upload).
+function CudaFVSolver:initCodeModules()
+	CudaFVSolver.super.initCodeModules(self)
+	for _,name in ipairs{'calcLR', 'calcFlux', 'calcDerivFromFlux'} do
+		local sym = self.symbols[name]
+		if sym then self.solverModulesEnabled[sym] = nil end
+	end
+end
+
+-- SolverBase's program build only: the GridSolver and FiniteVolumeSolver
+-- overrides (gridsolver.lua:444-456, fvsolver.lua:213-222) would look up the
+-- kernels left out above
+function CudaFVSolver:refreshSolverProgram()
+	require 'hydro.solver.solverbase'.refreshSolverProgram(self)
+end
+
 -- whole UBuf (ghosts included) between the OpenCL buffer and the CUDA solver;
 -- real must be double for the plain form's ghost-inclusive I/O
 local function ubufHost(self)

@@ -1,6 +1,6 @@
 --[[
 LuaJIT ffi binding of libhydrocuda.so: the declarations of include/hydrocuda.h
-that the 'cuda' solver class uses.  Load with
+that the 'cuda' solver class and the request loop (hydro/serve.lua) use.  Load with
 
 	local hc = require 'hydrocuda_ffi'
 
@@ -75,6 +75,45 @@ int hc_solver_display(hc_solver* s, int var, int zero_border, double* out);
 int hc_solver_display_range(hc_solver* s, int var, double out[4]);
 int hc_render_defaults(int mode, hc_render* out);
 int hc_solver_render(hc_solver* s, const hc_render* r, unsigned char* rgba);
+typedef struct hc_init {
+	int kind;
+	int reserved;
+	unsigned long long seed;
+	double p[16];
+} hc_init;
+typedef struct hc_batch_desc {
+	int precision;
+	int flux_limiter;
+	int recon;
+	int slope_limiter;
+	int integrator;
+	int max_slots;
+	size_t hbm_budget;
+	int flux;
+	int hllc_method;
+} hc_batch_desc;
+typedef struct hc_done {
+	int slot;
+	int status;
+	unsigned long long tag;
+	long long steps;
+	double t;
+} hc_done;
+typedef struct hc_batch hc_batch;
+int hc_init_defaults(int kind, hc_init* out);
+int hc_batch_create(hc_context* ctx, const hc_batch_desc* desc, hc_batch** out);
+int hc_batch_destroy(hc_batch* b);
+int hc_batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout, double t_end, long long max_steps, unsigned long long tag, int* slot);
+int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* init, double t_end, long long max_steps, unsigned long long tag, int* slot);
+int hc_batch_step(hc_batch* b, int steps, int* n_active);
+int hc_batch_step_async(hc_batch* b, int steps);
+int hc_batch_wait(hc_batch* b, int* n_active);
+int hc_batch_poll(hc_batch* b, hc_done* out, int cap, int* n_out);
+int hc_batch_list(hc_batch* b, hc_done* out, int cap, int* n_out);
+int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout);
+int hc_batch_retire(hc_batch* b, int slot);
+int hc_batch_autotune(hc_batch* b, const char* cache_path);
+int hc_batch_set_schedule(hc_batch* b, int dim, int variant);
 ]]
 
 local here = debug.getinfo(1, 'S').source:match'^@(.*)/[^/]*$' or '.'
@@ -103,6 +142,9 @@ M.fluxIndex = {roe = 0, hll = 1, rusanov = 2, ['euler-hllc'] = 3}
 M.reconIndex = {['piecewise constant'] = 1, ['plm cons'] = 2, ['plm prim'] = 3, ['plm athena'] = 4}
 M.precisionIndex = {['f64 plain'] = 0, f64 = 1, f32 = 2}
 M.LAYOUT_AOS6_F64 = 0
+M.initKind = {sod = 0, blast = 1, quadrant = 2, ['kelvin-helmholtz'] = 3}
+M.ERR_BUDGET = -4
+M.ERR_NO_SLOT = -5
 M.renderMode = {heatmap = 0, volume = 1, lic = 2, slices = 3}
 
 function M.check(code)

@@ -52,7 +52,7 @@ def test_declared_functions_match_the_header():
         assert decl == hdr[name], (decl, hdr[name])
 
 
-@pytest.mark.parametrize("name", ["hc_solver_desc", "hc_render"])
+@pytest.mark.parametrize("name", ["hc_solver_desc", "hc_render", "hc_init", "hc_batch_desc", "hc_done"])
 def test_structs_match_the_header(name):
     assert _struct_fields(_cdef(), name) == _struct_fields(_header(), name)
 

@@ -70,6 +70,21 @@ def workload(count=COUNT, seed=4, rank=0):
     return out
 
 
+def aggregate(elapsed, credited, dist):
+    """The whole job's clock and work over the ranks: the slowest rank's timed
+    region (max) and every rank's credited cell-updates (sum).  `dist` None:
+    one rank."""
+    if not dist:
+        return elapsed, credited
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(credited)], dtype=torch.float64, device=dev)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(c.item())
+
+
 def soa5_f32(hc, args, q):
     cons = hc.quadrant_state(args, q)
     return np.ascontiguousarray(cons[:, :5].T, dtype=np.float32)
@@ -307,16 +322,7 @@ def main():
         credited += cells_of[slot] * n
         full += n == args.steps and e["status"] == 0
         bad += e["status"] != 0
-    elapsed = total_ms / 1e3
-    if dist:
-        import torch
-        dev = "cuda" if torch.cuda.is_available() else "cpu"
-        t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-        c = torch.tensor([float(credited)], dtype=torch.float64, device=dev)
-        dist.all_reduce(c, op=dist.ReduceOp.SUM)
-        credited = int(c.item())
+    elapsed, credited = aggregate(total_ms / 1e3, credited, dist)
     value = credited / elapsed
     work_check = {"instances": len(after), "stepped_every_update": full, "status_nonzero": bad,
                   "credited_cell_updates": credited}

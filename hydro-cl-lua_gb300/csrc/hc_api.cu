@@ -56,6 +56,7 @@ struct hc_solver {
     FusedSet* fused = nullptr;
     double t = 0;           // plain form: SolverBase.t (a Lua double in the reference)
     long long steps = 0;
+    int next_stage = 0;     // fused forms: the stage hc_solver_stage runs next (0: between updates)
     int plain_status = HC_OK;   // plain form: first non-finite dt seen
 };
 
@@ -426,6 +427,7 @@ int hc_solver_calc_dt(hc_solver* s, double* dt) {
 
 int hc_solver_step(hc_solver* s, double dt) {
     if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    if (s->next_stage) return fail(HC_ERR_STATE, "an update run stage by stage is in progress");
     if (!(dt >= 0) || !std::isfinite(dt)) return fail(HC_ERR_INVALID, "dt must be finite and non-negative");
     HC_CHECK(use_device(s->ctx));
     if (s->plain) {
@@ -446,8 +448,39 @@ static int solver_status(hc_solver* s) {
     return HC_OK;
 }
 
+int hc_solver_stage(hc_solver* s, double dt) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    if (!(dt >= 0) || !std::isfinite(dt)) return fail(HC_ERR_INVALID, "dt must be finite and non-negative");
+    if (s->plain) return fail(HC_ERR_INVALID, "the plain form steps whole updates (hc_solver_step)");
+    HC_CHECK(use_device(s->ctx));
+    HC_CHECK(fused_stage(s->fused, 0, dt, s->next_stage));
+    s->next_stage = (s->next_stage + 1) % fused_num_stages(s->fused);
+    return fused_sync(s->fused);
+}
+
+int hc_solver_num_stages(hc_solver* s, int* n) {
+    if (!s || !n) return fail(HC_ERR_INVALID, "NULL argument");
+    if (s->plain) return fail(HC_ERR_INVALID, "the plain form steps whole updates (hc_solver_step)");
+    *n = fused_num_stages(s->fused);
+    return HC_OK;
+}
+
+static int solver_slab(hc_solver* s, int axis, int side, double* buf, int dir) {
+    if (!s || !buf) return fail(HC_ERR_INVALID, "NULL argument");
+    if (s->plain) return fail(HC_ERR_INVALID, "the plain form steps whole updates: slabs are for the fused forms");
+    HC_CHECK(use_device(s->ctx));
+    return fused_slab(s->fused, 0, s->next_stage, axis, side, dir, buf);
+}
+
+int hc_solver_get_slab(hc_solver* s, int axis, int side, double* out) { return solver_slab(s, axis, side, out, 1); }
+
+int hc_solver_set_slab(hc_solver* s, int axis, int side, const double* in) {
+    return solver_slab(s, axis, side, const_cast<double*>(in), 0);
+}
+
 int hc_solver_update(hc_solver* s, double* dt_out) {
     if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    if (s->next_stage) return fail(HC_ERR_STATE, "an update run stage by stage is in progress");
     HC_CHECK(use_device(s->ctx));
     if (s->plain) {
         double dt;

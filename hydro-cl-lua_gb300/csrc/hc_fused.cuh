@@ -1296,6 +1296,35 @@ __global__ void k_xfer(const DevInst* inst, int slot, int buf, void* staging, in
     }
 }
 
+// The two layers next to face (axis, side) of one slot's buffer, as AoS-6
+// doubles (ePot 0) x-fastest over the 2-layer slab, to staging (dir 1: the
+// two interior layers next to the face) or from it (dir 0: the two ghost
+// layers beyond the face).  A grid cut into slabs across ranks exchanges
+// these between neighbours before every stage.
+template <typename T, int DIM>
+__global__ void k_slab(const DevInst* inst, int slot, int buf, int axis, int side, int dir, double* staging) {
+    const DevInst& I = inst[slot];
+    T* base = reinterpret_cast<T*>(I.buf[buf]);
+    int ext[3] = {I.n[0], I.n[1], I.n[2]};
+    ext[axis] = kG;
+    long long const n = (long long)ext[0] * ext[1] * ext[2];
+    int const N = I.n[axis];
+    // first layer's coordinate along the axis
+    int const c0 = dir ? (side ? N - kG : 0) : (side ? N : -kG);
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        int c[3] = {(int)(k % ext[0]), (int)((k / ext[0]) % ext[1]), (int)(k / ((long long)ext[0] * ext[1]))};
+        c[axis] += c0;
+        long long const idx = padIndex<DIM>(I, c[0], c[1], c[2]);
+        double* h = staging + 6 * k;
+        if (dir) {
+            for (int f = 0; f < 5; ++f) h[f] = (double)base[f * I.plane + idx];
+            h[5] = 0.;
+        } else {
+            for (int f = 0; f < 5; ++f) base[f * I.plane + idx] = (T)h[f];
+        }
+    }
+}
+
 // A state set-up in one pass (admission, resetState, setState): staging ->
 // interior with the layout conversion of k_xfer, constrainU when `reset`, the
 // ghosts that copy one interior cell (periodic / mirror / freeflow) and the
@@ -1406,6 +1435,9 @@ struct AuxLauncher {
     void (*sums)(const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s);
     // linear / quadratic ghosts of a stage's output on every stepping instance of this dimension
     void (*extrap_stage)(const DevInst* inst, const DevCtl* ctl, int nslots, int out_buf, int rot_buf, cudaStream_t s);
+    // k_slab over `cells` slab cells
+    void (*slab)(const DevInst* inst, int slot, int buf, int axis, int side, int dir, double* staging, long long cells,
+                 cudaStream_t s);
 };
 
 void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>& aux);

@@ -341,9 +341,12 @@ static int validate(const FusedSet* f, const hc_solver_desc& d) {
         if (d.n[k] > (1 << 24)) return fail(HC_ERR_INVALID, "grid axis too large");
         if (!(d.maxs[k] > d.mins[k])) return fail(HC_ERR_INVALID, "maxs must exceed mins");
     }
+    // 'none' leaves a side's ghost cells as they are (gridsolver.lua's
+    // BoundaryNone): a caller fills them, as a grid cut into slabs does with
+    // its neighbours' layers
     for (int k = 0; k < 2 * d.dim; ++k)
-        if (d.boundary[k] == HC_BOUNDARY_NONE || d.boundary[k] < 0 || d.boundary[k] >= HC_NUM_BOUNDARIES)
-            return fail(HC_ERR_INVALID, "the fused form supports periodic, mirror, freeflow, linear and quadratic boundaries");
+        if (d.boundary[k] < 0 || d.boundary[k] >= HC_NUM_BOUNDARIES)
+            return fail(HC_ERR_INVALID, "the fused form supports none, periodic, mirror, freeflow, linear and quadratic boundaries");
     for (int k = 0; k < d.dim; ++k)
         if ((d.boundary[2 * k] == HC_BOUNDARY_PERIODIC) != (d.boundary[2 * k + 1] == HC_BOUNDARY_PERIODIC))
             return fail(HC_ERR_INVALID, "periodic boundaries must be periodic on both sides of an axis");
@@ -619,6 +622,19 @@ static int rebuild_items(FusedSet* f) {
             for (int y = 0; y < nty; ++y)
                 for (int x = 0; x < ntx; ++x) items[S.dim - 1].push_back(make_int4(s, x, y, z));
     }
+    // a marching schedule's item costs its segment's rows: full segments
+    // first, the shorter ones at the grid tops last, so the launch's tail is
+    // short (stable: neighbouring strips stay together for their halo rows in L2)
+    for (int d = 0; d < 3; ++d) {
+        const StageLauncher* L = f->launcher[d];
+        if (!L || !L->march) continue;
+        auto rowsOf = [&](const int4& it) {
+            int const ny = f->slots[it.x].inst.n[1];
+            return std::min(L->ty, ny - it.z * L->ty);
+        };
+        std::stable_sort(items[d].begin(), items[d].end(),
+                         [&](const int4& a, const int4& b) { return rowsOf(a) > rowsOf(b); });
+    }
     int mask = 0;
     for (int d = 0; d < 3; ++d) {
         size_t const n = items[d].size();
@@ -773,6 +789,59 @@ int fused_step_dt(FusedSet* f, int slot, double dt) {
     HC_CHECK(launch_stages(f, f->plan[0], 1 << (S.dim - 1)));
     fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 0, f->rotates, f->betas, f->d_work);
     HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+int fused_num_stages(const FusedSet* f) { return f->plan[0].n_stages; }
+
+// Stage `stage` of one update of one slot with the update's dt: the first
+// stage sets the step's coefficients, the last one completes the step (t is
+// not advanced, as in fused_step_dt).
+int fused_stage(FusedSet* f, int slot, double dt, int stage) {
+    HC_CHECK(rebuild_items(f));
+    const Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    const IntegratorPlan& P = f->plan[0];
+    if (stage < 0 || stage >= P.n_stages) return fail(HC_ERR_INVALID, "stage");
+    if (stage == 0) fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 1, f->rotates, f->betas, f->d_work);
+    IntegratorPlan one;
+    std::memset(&one, 0, sizeof(one));
+    one.n_stages = 1;
+    one.stage[0] = P.stage[stage];
+    HC_CHECK(launch_stages(f, one, 1 << (S.dim - 1)));
+    if (stage == P.n_stages - 1)
+        fz::k_set_dt<<<1, 1, 0, f->stream>>>(f->d_ctl, f->d_inst, slot, dt, 0, f->rotates, f->betas, f->d_work);
+    HC_CUDA(cudaGetLastError());
+    return HC_OK;
+}
+
+// The two layers next to face (axis, side) of the buffer stage `stage` reads,
+// as AoS-6 doubles: read (dir 1: the interior layers next to the face) or
+// written (dir 0: the ghost layers beyond it).
+int fused_slab(FusedSet* f, int slot, int stage, int axis, int side, int dir, double* host) {
+    Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    if (axis < 0 || axis >= S.dim || side < 0 || side > 1) return fail(HC_ERR_INVALID, "face");
+    if (S.inst.n[axis] < kG) return fail(HC_ERR_INVALID, "the axis has fewer cells than ghost layers");
+    const IntegratorPlan& P = f->plan[0];
+    int rot = 0;
+    if (f->rotates) {
+        HC_CUDA(cudaMemcpyAsync(&rot, &f->d_ctl[slot].rot, sizeof(int), cudaMemcpyDeviceToHost, f->stream));
+        HC_CUDA(cudaStreamSynchronize(f->stream));
+    }
+    // slotBuf on the host: a rotated slot sees buffers 0 and rot_buf exchanged
+    int const b0 = P.stage[stage].in_buf;
+    int const buf = rot ? (b0 == 0 ? f->rot_buf : (b0 == f->rot_buf ? 0 : b0)) : b0;
+    long long cells = (long long)kG;
+    for (int k = 0; k < S.dim; ++k) if (k != axis) cells *= S.inst.n[k];
+    size_t const bytes = (size_t)cells * 6 * sizeof(double);
+    HC_CHECK(ensure_staging(f, bytes));
+    const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
+    if (dir == 0) HC_CUDA(cudaMemcpyAsync(f->staging, host, bytes, cudaMemcpyHostToDevice, f->stream));
+    A->slab(f->d_inst, slot, buf, axis, side, dir, static_cast<double*>(f->staging), cells, f->stream);
+    HC_CUDA(cudaGetLastError());
+    if (dir == 1) HC_CUDA(cudaMemcpyAsync(host, f->staging, bytes, cudaMemcpyDeviceToHost, f->stream));
+    HC_CUDA(cudaStreamSynchronize(f->stream));
     return HC_OK;
 }
 

@@ -162,6 +162,13 @@ int fused_steps_timed(FusedSet* f, int steps, double* stage_ms, int n_stage_ms, 
 // One update of the given slot's instance with an explicit dt (-1: CFL dt).
 int fused_step_dt(FusedSet* f, int slot, double dt);
 int fused_calc_dt(FusedSet* f, int slot, double* dt);
+// one Runge-Kutta stage of a slot's update (the first sets the step's
+// coefficients, the last completes the step; t is not advanced)
+int fused_stage(FusedSet* f, int slot, double dt, int stage);
+int fused_num_stages(const FusedSet* f);
+// the two layers next to face (axis, side) of the buffer stage `stage` reads,
+// as AoS-6 doubles on the host: dir 1 reads the interior layers, dir 0 writes the ghosts
+int fused_slab(FusedSet* f, int slot, int stage, int axis, int side, int dir, double* host);
 int fused_boundary(FusedSet* f, int slot);
 int fused_constrain_u(FusedSet* f, int slot);
 struct SlotInfo { double t; double dt; long long steps; int active; int done; int status; };

@@ -13,11 +13,13 @@ exchange per derivative evaluation the decomposed run reproduces the
 single-domain run exactly; with one exchange per update (the reference's
 choice) that holds for forward Euler only.
 
-The functions work on host arrays in the reference's layout (AoS-6 cons_t,
-x-fastest, ghosts included) over ``torch.distributed`` point-to-point
-messages, so the same code serves CPU ranks (gloo) and, with device
-tensors, NCCL.  Every box in this build has one GPU, so the GPU path is not
-exercised here; the tests run the CPU path against the oracle.
+Two forms of the exchange: ``exchange_ghosts`` on a whole host array in the
+reference's layout (AoS-6 cons_t, x-fastest, ghosts included), for the
+oracle; and ``exchange_slabs`` / ``update`` on a libhydrocuda solver, through
+hc_solver_get_slab / hc_solver_set_slab / hc_solver_stage, so each rank's slab
+lives on its device and only the two-layer slabs next to the internal faces
+cross to the host and over ``torch.distributed`` point-to-point messages
+(gloo here; the slabs are small, host-staged).
 """
 import numpy as np
 
@@ -119,6 +121,56 @@ def exchange_ghosts(full, args, rank, world, dist):
         r.wait()
     for sl, recv, _ in bufs:
         g[take(sl)] = recv.numpy()
+
+
+def _neighbours(args, rank, world):
+    periodic = bool(args.get("_periodic_split", False))
+    down = rank - 1 if rank > 0 else (world - 1 if periodic else None)
+    up = rank + 1 if rank < world - 1 else (0 if periodic else None)
+    return down, up
+
+
+def exchange_slabs(solver, args, rank, world, dist):
+    """Before a stage: this slab's two layers next to each internal face go to
+    the neighbour across it, and the neighbour's become this slab's ghosts, in
+    the state the solver's next stage reads (tags as in exchange_ghosts)."""
+    import torch
+    ax = int(args["dim"]) - 1
+    down, up = _neighbours(args, rank, world)
+    reqs, recvs = [], []
+    if down is not None:
+        send = torch.from_numpy(solver.get_slab(ax, 0))
+        recv = torch.empty_like(send)
+        reqs.append(dist.isend(send, down, tag=1))
+        reqs.append(dist.irecv(recv, down, tag=2))
+        recvs.append((0, recv, send))
+    if up is not None:
+        send = torch.from_numpy(solver.get_slab(ax, 1))
+        recv = torch.empty_like(send)
+        reqs.append(dist.isend(send, up, tag=2))
+        reqs.append(dist.irecv(recv, up, tag=1))
+        recvs.append((1, recv, send))
+    for r in reqs:
+        r.wait()
+    for side, recv, _ in recvs:
+        solver.set_slab(ax, side, recv.numpy())
+
+
+def update(solver, args, rank, world, dist):
+    """One update of the decomposed grid on a libhydrocuda solver (fused form):
+    the ranks' minimum dt, then for every Runge-Kutta stage the slab exchange
+    and the stage; t advances by dt.  Returns dt."""
+    dt = allreduce_min(solver.calcDT(), dist)
+    for _ in range(solver.num_stages):
+        exchange_slabs(solver, args, rank, world, dist)
+        solver.stage(dt)
+    solver.t = solver.t + dt
+    return dt
+
+
+def solver_args(sargs):
+    """slab_args without the decomposition's own keys (for hydrocuda.Solver)."""
+    return {k: v for k, v in sargs.items() if not k.startswith("_")}
 
 
 def allreduce_min(value, dist):

@@ -150,6 +150,10 @@ PROTOTYPES = {
     "hc_solver_calc_dt": (_ip, [_vp, _dp]),
     "hc_solver_step": (_ip, [_vp, ctypes.c_double]),
     "hc_solver_update": (_ip, [_vp, _dp]),
+    "hc_solver_stage": (_ip, [_vp, ctypes.c_double]),
+    "hc_solver_num_stages": (_ip, [_vp, ctypes.POINTER(ctypes.c_int)]),
+    "hc_solver_get_slab": (_ip, [_vp, _ip, _ip, _dp]),
+    "hc_solver_set_slab": (_ip, [_vp, _ip, _ip, _dp]),
     "hc_solver_run_until": (_ip, [_vp, ctypes.c_double, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]),
     "hc_solver_get_time": (_ip, [_vp, _dp]),
     "hc_solver_set_time": (_ip, [_vp, ctypes.c_double]),
@@ -485,6 +489,36 @@ class Solver:
         dt = ctypes.c_double()
         _check(self.L.hc_solver_update(self.h, ctypes.byref(dt)))
         return dt.value
+
+    # one grid cut into slabs (see hc_solver_stage in the header)
+    @property
+    def num_stages(self):
+        n = ctypes.c_int()
+        _check(self.L.hc_solver_num_stages(self.h, ctypes.byref(n)))
+        return n.value
+
+    def stage(self, dt):
+        """The next Runge-Kutta stage of the update with the update's dt (hc_solver_stage)."""
+        _check(self.L.hc_solver_stage(self.h, float(dt)))
+
+    def _slab_cells(self, axis):
+        n = 2
+        for k in range(self.dim):
+            if k != axis:
+                n *= self.gridSize[k]
+        return n
+
+    def get_slab(self, axis, side):
+        """The two interior layers next to face (axis, side) of the state the next stage reads,
+        (cells, 6) float64 x-fastest over the two-layer slab."""
+        out = np.empty((self._slab_cells(axis), 6), dtype=np.float64)
+        _check(self.L.hc_solver_get_slab(self.h, int(axis), int(side), out.ctypes.data_as(_dp)))
+        return out
+
+    def set_slab(self, axis, side, cons):
+        """Writes the two ghost layers beyond face (axis, side) of the state the next stage reads."""
+        a = np.ascontiguousarray(cons, dtype=np.float64).reshape(self._slab_cells(axis), 6)
+        _check(self.L.hc_solver_set_slab(self.h, int(axis), int(side), a.ctypes.data_as(_dp)))
 
     def run_until(self, t_end, max_steps=(1 << 62)):
         n = ctypes.c_longlong()

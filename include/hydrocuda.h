@@ -242,6 +242,33 @@ int hc_solver_calc_dt(hc_solver* s, double* dt);
 int hc_solver_step(hc_solver* s, double dt);
 /* SolverBase:update() (solverbase.lua:3026): calcDT, step, t += dt, boundary. */
 int hc_solver_update(hc_solver* s, double* dt_out);
+/* ---- one grid cut into slabs across devices or ranks --------------------------
+ *
+ * The reference's multi-device solver (hydro/solver/choppedup.lua) cuts a
+ * grid into blocks, copies the ghost layers between neighbouring blocks
+ * (syncBorders, choppedup.lua:193-230) and takes the minimum of the blocks' dt
+ * on the host (Chopped:update, choppedup.lua:344-400), once per update.  These
+ * calls let the same happen per Runge-Kutta stage, which is what reproduces
+ * the single-domain result for every integrator: give each slab's solver the
+ * boundary "none" on its internal faces, take the ranks' minimum of
+ * hc_solver_calc_dt, then for each stage exchange the slabs next to the
+ * internal faces and run the stage.  Fused forms only (HC_ERR_INVALID on the
+ * plain form, which steps whole updates).
+ *
+ * hc_solver_stage runs the next stage of the update with the update's dt (the
+ * first call sets up the step, the last one completes it; t is not advanced,
+ * as with hc_solver_step); hc_solver_step / hc_solver_update refuse while an
+ * update is part done (HC_ERR_STATE).  hc_solver_num_stages gives the
+ * integrator's stage count.  hc_solver_get_slab copies the two interior
+ * layers next to face (axis 0..dim-1, side 0: min, 1: max) of the state the
+ * next stage reads to the host; hc_solver_set_slab writes the two ghost
+ * layers beyond that face.  Both as cons_t (6 doubles per cell, ePot 0),
+ * x-fastest over the two-layer slab (extent 2 along `axis`, the interior
+ * extents along the others). */
+int hc_solver_stage(hc_solver* s, double dt);
+int hc_solver_num_stages(hc_solver* s, int* n);
+int hc_solver_get_slab(hc_solver* s, int axis, int side, double* out);
+int hc_solver_set_slab(hc_solver* s, int axis, int side, const double* in);
 /* The App loop: while t < t_end and steps < max_steps, update().  The test is
  * made before each update, so the final step overshoots t_end (app.lua:1590). */
 int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long long* steps_done);

@@ -96,3 +96,56 @@ def test_instances_shard_without_overlap():
     items = list(range(37))
     parts = [decomp.shard_instances(items, r, 4) for r in range(4)]
     assert sorted(sum(parts, [])) == items
+
+
+def _bench_rank(rank, world, port, out_dir):
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (root, os.path.join(root, "hydro-cl-lua_gb300")):
+        sys.path.insert(0, p)
+    import torch.distributed as dist
+    import bench
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    work = bench.workload(count=6, rank=rank)
+    sizes = [a["gridSize"][0] for a, _ in work]
+    # each rank's own clock and credited work, as bench.py's main has them
+    elapsed, credited = bench.aggregate(1.0 + rank, 1000 * (rank + 1), dist)
+    np.save(os.path.join(out_dir, "bench%d.npy" % rank),
+            np.array([elapsed, credited] + sizes, dtype=np.float64))
+    quads = [q for _, q in work]
+    import pickle
+    with open(os.path.join(out_dir, "quads%d.pkl" % rank), "wb") as f:
+        pickle.dump(quads, f)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_bench_replicas_aggregate_over_ranks(tmp_path):
+    """bench.py's WORLD_SIZE=2 path on gloo ranks: every rank holds its own
+    instances (weak scaling: the same count, different seeds), and the job's
+    value is every rank's credited work over the slowest rank's clock."""
+    import pickle
+    import torch.multiprocessing as mp
+    port = free_port()
+    mp.start_processes(_bench_rank, args=(2, port, str(tmp_path)), nprocs=2, join=True, start_method="spawn")
+    r0, r1 = (np.load(tmp_path / ("bench%d.npy" % r)) for r in range(2))
+    for r in (r0, r1):
+        assert r[0] == 2.0                      # max of the ranks' 1.0 and 2.0 s
+        assert r[1] == 3000                     # 1000 + 2000 cell-updates
+    assert len(r0) == len(r1) == 2 + 6
+    q0, q1 = (pickle.load(open(tmp_path / ("quads%d.pkl" % r), "rb")) for r in range(2))
+    assert all(repr(a) != repr(b) for a, b in zip(q0, q1))   # different instances per rank
+
+
+def test_bench_reference_arm_runs_on_rank_zero_only():
+    """Under torchrun the reference arm's ranks other than 0 exit 0 without work or output."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    p = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--gpus", "2"],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert p.stdout.strip() == ""

@@ -622,15 +622,17 @@ static int rebuild_items(FusedSet* f) {
             for (int y = 0; y < nty; ++y)
                 for (int x = 0; x < ntx; ++x) items[S.dim - 1].push_back(make_int4(s, x, y, z));
     }
-    // a marching schedule's item costs its segment's rows: full segments
-    // first, the shorter ones at the grid tops last, so the launch's tail is
-    // short (stable: neighbouring strips stay together for their halo rows in L2)
+    // a marching schedule's item costs its segment's rows (times its planes
+    // in 3D): full segments first, the shorter ones at the grid tops last, so
+    // the launch's tail is short (stable: neighbouring strips stay together
+    // for their halo rows in L2)
     for (int d = 0; d < 3; ++d) {
         const StageLauncher* L = f->launcher[d];
         if (!L || !L->march) continue;
         auto rowsOf = [&](const int4& it) {
-            int const ny = f->slots[it.x].inst.n[1];
-            return std::min(L->ty, ny - it.z * L->ty);
+            const DevInst& I = f->slots[it.x].inst;
+            int const rows = std::min(L->ty, I.n[1] - it.z * L->ty);
+            return d == 2 ? rows * std::min(L->tz, I.n[2] - it.w * L->tz) : rows;
         };
         std::stable_sort(items[d].begin(), items[d].end(),
                          [&](const int4& a, const int4& b) { return rowsOf(a) > rowsOf(b); });
@@ -1103,6 +1105,7 @@ void register_f32_d3b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3c(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_m2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_m3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -1120,6 +1123,7 @@ void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>
     register_f32_d3c(st, aux);
     register_f32_d3(st, aux);
     register_f32_m2(st, aux);
+    register_f32_m3(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);
     register_f64_d3(st, aux);

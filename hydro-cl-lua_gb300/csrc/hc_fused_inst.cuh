@@ -5,6 +5,7 @@
 
 #include "hc_fused.cuh"
 #include "hc_march.cuh"
+#include "hc_march3.cuh"
 
 namespace hc {
 namespace fz {
@@ -100,6 +101,56 @@ void add_march2(std::vector<StageLauncher>& v) {
             if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
             int n = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NW * 32, Cfg::SMEM) != cudaSuccess) return -1;
+            occ = n < occ ? n : occ;
+        }
+        return occ;
+    };
+    v.push_back(sl);
+}
+
+// A 3D marching schedule (hc_march3.cuh): tiles of 30 columns by NWY - 1
+// rows (NWY warps per CTA) marching up segments of D planes, NB plane buffers,
+// the slope limiter SLOPE compiled in (-1: read at run time), OCC CTAs per SM.
+template <int VAR, int NWY, int D, int NB, int SLOPE, int OCC>
+void add_march3(std::vector<StageLauncher>& v) {
+    using Cfg = March3Cfg<NWY, NB>;
+    StageLauncher sl;
+    sl.precision = HC_F32_FUSED;
+    sl.dim = 3;
+    sl.recon = HC_RECON_PLM_CONS;
+    sl.lim = false;
+    sl.slope = SLOPE;
+    sl.variant = VAR;
+    sl.tx = kStripW;
+    sl.ty = NWY - 1;
+    sl.tz = D;
+    sl.nthreads = NWY * 32;
+    sl.seg = D;
+    sl.unroll = 1;
+    sl.min_ctas = OCC;
+    sl.lanes = 1;
+    sl.flux = HC_FLUX_ROE;
+    sl.box[0] = kMarchBW;
+    sl.box[1] = NWY + 3;
+    sl.box[2] = 1;
+    sl.march = 1;
+    sl.smem = Cfg::SMEM;
+    sl.launch = [](const StageArgs& a, int slopeLim, int fluxLim, int grid, cudaStream_t s) {
+        switch (marchEpi(a.st)) {
+        case 1: k_march3<NWY, D, NB, SLOPE, OCC, 1><<<grid, NWY * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim); break;
+        case 2: k_march3<NWY, D, NB, SLOPE, OCC, 2><<<grid, NWY * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim); break;
+        case 3: k_march3<NWY, D, NB, SLOPE, OCC, 3><<<grid, NWY * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim); break;
+        default: k_march3<NWY, D, NB, SLOPE, OCC, 0><<<grid, NWY * 32, Cfg::SMEM, s>>>(a, slopeLim, fluxLim);
+        }
+    };
+    sl.occupancy = []() -> int {
+        void (*ks[4])(StageArgs, int, int) = {k_march3<NWY, D, NB, SLOPE, OCC, 0>, k_march3<NWY, D, NB, SLOPE, OCC, 1>,
+                                              k_march3<NWY, D, NB, SLOPE, OCC, 2>, k_march3<NWY, D, NB, SLOPE, OCC, 3>};
+        int occ = 1 << 30;
+        for (auto k : ks) {
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM) != cudaSuccess) return -1;
+            int n = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, NWY * 32, Cfg::SMEM) != cudaSuccess) return -1;
             occ = n < occ ? n : occ;
         }
         return occ;

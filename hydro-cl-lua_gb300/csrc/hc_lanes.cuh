@@ -445,40 +445,46 @@ __device__ __forceinline__ void roe(V* F, const Eos& s, const C5<V>& UL, const C
     }
 }
 
-// The Roe flux of two interfaces at once on register pairs, in the upwind
-// form F(UL) + R min(Lambda, 0) L.(UR - UL), operation for operation as
-// roe<float> evaluates it where the Roe average is the plain one.  Returns
-// whether both lanes have the plain average (no vacuum side, enthalpy above
-// its floor, averaged density at least rhoMin); where a lane has not, F is
-// not that lane's flux and the caller evaluates roe<float> for it.
-__device__ __forceinline__ bool roeUp2(float2* F, const Eos& s, const C5<float2>& UL, const C5<float2>& UR) {
-    B2 const lv = lt(UL.u[0], splat<float2>(1e-5f)), rv = lt(UR.u[0], splat<float2>(1e-5f));
-    Eig<float2> e;
-    float2 PL, invL;
-    B2 low;
-    float2 const rho = eigenRoe(e, s, UL, UR, PL, invL, low);
+// The Roe flux of one interface (V = float) or two at once on register pairs
+// (V = float2, roeUp2), in the upwind form F(UL) + R min(Lambda, 0)
+// L.(UR - UL), operation for operation as roe<float> evaluates it where the
+// Roe average is the plain one.  Returns whether every lane has the plain
+// average (no vacuum side, enthalpy above its floor, averaged density at
+// least rhoMin); where a lane has not, F is not that lane's flux and the
+// caller evaluates roe<float> for it.
+template <typename V>
+__device__ __forceinline__ bool roeUp(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+    Mask<V> const lv = lt(UL.u[0], splat<V>(1e-5f)), rv = lt(UR.u[0], splat<V>(1e-5f));
+    Eig<V> e;
+    V PL, invL;
+    Mask<V> low;
+    V const rho = eigenRoe(e, s, UL, UR, PL, invL, low);
     finishEig(e, s, rho);
-    float2 dU[5], dW[5], fe[5];
+    V dU[5], dW[5], fe[5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) dU[j] = sub(UR.u[j], UL.u[j]);
     left(dW, e, s, dU);
-    float2 const zero = splat<float2>(0.f);
-    float2 const c0 = vmin(sub(e.vn, e.Cs), zero);
-    float2 const c1 = vmin(e.vn, zero);
-    float2 const c4 = vmin(add(e.vn, e.Cs), zero);
+    V const zero = splat<V>(0.f);
+    V const c0 = vmin(sub(e.vn, e.Cs), zero);
+    V const c1 = vmin(e.vn, zero);
+    V const c4 = vmin(add(e.vn, e.Cs), zero);
     fe[0] = mul(c0, dW[0]);
     fe[1] = mul(c1, dW[1]);
     fe[2] = mul(c1, dW[2]);
     fe[3] = mul(c1, dW[3]);
     fe[4] = mul(c4, dW[4]);
     right(F, e, fe);
-    float2 const vn = mul(UL.u[1], invL);
+    V const vn = mul(UL.u[1], invL);
     F[0] = add(F[0], UL.u[1]);
     F[1] = add(F[1], fma(UL.u[1], vn, PL));
     F[2] = fma(UL.u[2], vn, F[2]);
     F[3] = fma(UL.u[3], vn, F[3]);
     F[4] = fma(add(UL.u[4], PL), vn, F[4]);
     return !any(lv || rv || low || e.ident);
+}
+
+__device__ __forceinline__ bool roeUp2(float2* F, const Eos& s, const C5<float2>& UL, const C5<float2>& UR) {
+    return roeUp<float2>(F, s, UL, UR);
 }
 
 // HLLC flux (hydro/flux/euler-hllc.cl, 2012 Toro; waves as hll) in the

@@ -103,6 +103,7 @@ template <typename T> struct Eos {
     T gamma, g1, rhoMin, PMin;
     int fluxLimiter, slopeLimiter;
     int hllcMethod;
+    T entropyFactor;   // the Roe flux's entropy fix factor, 0: off
 };
 
 // A conserved state in the interface frame: rho, m_n, m_t1, m_t2, ETotal.
@@ -252,7 +253,14 @@ __device__ __forceinline__ void roeLimited(T* F, const Eos<T>& s, const C5<T>& U
     T const vn = C.e.vn, Cs = C.e.Cs;
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
-        T const lambda = j == 0 ? vn - Cs : (j == 4 ? vn + Cs : vn);
+        T lambda = j == 0 ? vn - Cs : (j == 4 ? vn + Cs : vn);
+        if (s.entropyFactor != T(0)) {
+            // useEntropyFluxFix (roe.cl:83-101)
+            T const dws = s.entropyFactor * Cs;
+            if (M<T>::abs_(lambda) < dws)
+                lambda = (lambda > T(0) ? T(1) : (lambda < T(0) ? T(-1) : lambda)) * T(.5) *
+                         (M<T>::div(lambda * lambda, dws) + dws);
+        }
         T const sgn = lambda >= T(0) ? T(1) : T(-1);
         T rEig;
         if (C.dW[j] == T(0)) rEig = T(0);

@@ -64,6 +64,10 @@ struct DevInst {
     int stop_on_error;     // 1 (batched solves): a non-finite state or dt ends the instance
     // the same constants in FP32, converted once on the host
     float f_gamma, f_g1, f_rhoMin, f_PMin, f_invg1, f_area[3], f_gdx[3];
+    int entropyFix;            // Roe: useEntropyFluxFix with entropyFactor (f_: 0 when off)
+    double entropyFactor;
+    float f_entropyFactor;
+    double fixedCons[6][5];    // HC_BOUNDARY_FIXED sides: the ghost cells' state
     void* buf[kMaxBufs];
     void* dbuf[kMaxDBufs];
 };
@@ -295,6 +299,9 @@ __device__ __forceinline__ void makeTileK(TileK<T>& k, const DevInst& I, const D
     }
     k.fe.fluxLimiter = fluxLim;
     k.fe.slopeLimiter = slopeLim;
+    k.fe.entropyFactor = sizeof(T) == 4 ? (T)I.f_entropyFactor : (T)(I.entropyFix ? I.entropyFactor : 0.);
+    k.re.entropyFix = I.entropyFix;
+    k.re.entropyFactor = I.entropyFactor;
     k.re.gamma = I.gamma;
     k.re.rhoMin = I.rhoMin;
     k.re.PMin = I.PMin;
@@ -709,7 +716,8 @@ template <typename T, int AXIS, int STRIDE, int LSTRIDE, int BOXN, int L, bool E
 __device__ __forceinline__ void sweepAny(const T* box, int base, const TileK<T>& K, Emit&& emit) {
     if constexpr (!EXACT && !LIM && sizeof(T) == 4) {
         using V = typename std::conditional<LANES == 2, float2, float>::type;
-        lanes::Eos const e{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon};
+        lanes::Eos const e{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon,
+                             (float)K.fe.entropyFactor};
         sweepLanes<V, AXIS, STRIDE, LSTRIDE, BOXN, L, PLM, SLOPE, UNR, FLUX>(
             box, base, e, SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter, K.zero[AXIS], emit);
     } else {
@@ -1006,7 +1014,8 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
                 else if (second) *reinterpret_cast<float2*>(p) = v;
                 else *p = lanes::lane(v, 0);
             };
-            lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon};
+            lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon,
+                             (float)K.fe.entropyFactor};
             V u[5], deriv[5];
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
@@ -1164,6 +1173,39 @@ __global__ void k_fill_ghosts(const DevInst* inst, int slot, int buf) {
         T u[5];
         for (int f = 0; f < 5; ++f) u[f] = base[f * I.plane + idx];
         scatterGhosts<T, DIM>(I, base, gx, gy, gz, u);
+    }
+}
+
+// The fixed boundaries (gridsolver.lua:746-765) of one instance: the two
+// ghost layers of every HC_BOUNDARY_FIXED side take the side's constant state
+// in each of the first `nbufs` state buffers, on the lines through the
+// interior (corner ghosts are never read).  No stage writes these ghosts, so
+// this runs once when the instance is set up.
+template <typename T, int DIM>
+__global__ void k_fixed_ghosts(const DevInst* inst, int slot, int nbufs) {
+    const DevInst& I = inst[slot];
+    long long const stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 1
+    for (int d = 0; d < DIM; ++d) {
+        int const o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+        long long const nface = (long long)I.n[o1] * I.n[o2];
+#pragma unroll 1
+        for (int mm = 0; mm < 2; ++mm) {
+            if (I.bc[2 * d + mm] != HC_BOUNDARY_FIXED) continue;
+            const double* const v = I.fixedCons[2 * d + mm];
+            for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nface * 2 * nbufs; k += stride) {
+                long long const cell = k % nface;
+                int const j = (int)((k / nface) % 2), b = (int)(k / (2 * nface));
+                int c[3];
+                c[o1] = (int)(cell % I.n[o1]);
+                c[o2] = (int)(cell / I.n[o1]);
+                c[d] = mm == 0 ? -1 - j : I.n[d] + j;
+                long long const idx = padIndex<DIM>(I, c[0], c[1], c[2]);
+                T* const base = reinterpret_cast<T*>(I.buf[b]);
+#pragma unroll
+                for (int f = 0; f < 5; ++f) base[f * I.plane + idx] = (T)v[f];
+            }
+        }
     }
 }
 
@@ -1435,6 +1477,8 @@ struct AuxLauncher {
     void (*sums)(const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s);
     // linear / quadratic ghosts of a stage's output on every stepping instance of this dimension
     void (*extrap_stage)(const DevInst* inst, const DevCtl* ctl, int nslots, int out_buf, int rot_buf, cudaStream_t s);
+    // k_fixed_ghosts on the first nbufs state buffers
+    void (*fixed_ghosts)(const DevInst* inst, int slot, int nbufs, cudaStream_t s);
     // k_slab over `cells` slab cells
     void (*slab)(const DevInst* inst, int slot, int buf, int axis, int side, int dir, double* staging, long long cells,
                  cudaStream_t s);

@@ -417,6 +417,13 @@ static bool has_extrap(const Slot& S) {
     return false;
 }
 
+// the instance has a fixed side (constant ghosts, set once)
+static bool has_fixed(const Slot& S) {
+    for (int k = 0; k < 2 * S.dim; ++k)
+        if (S.inst.bc[k] == HC_BOUNDARY_FIXED) return true;
+    return false;
+}
+
 // buffer holding a slot's current state
 static int state_buf(FusedSet* f, int slot) {
     if (!f->rotates) return 0;
@@ -559,6 +566,10 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     I.f_rhoMin = (float)d.rho_min;
     I.f_PMin = (float)d.p_min;
     I.f_invg1 = (float)(1. / (d.gamma - 1.));
+    I.entropyFix = d.entropy_fix != 0;
+    I.entropyFactor = d.entropy_fix_factor;
+    I.f_entropyFactor = d.entropy_fix ? (float)d.entropy_fix_factor : 0.f;
+    std::memcpy(I.fixedCons, d.fixed_cons, sizeof(I.fixedCons));
     for (int k = 0; k < 3; ++k) {
         I.f_area[k] = (float)I.area[k];
         I.f_gdx[k] = (float)I.grid_dx[k];
@@ -575,6 +586,8 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     c.active = 1;
     HC_CUDA(cudaMemcpyAsync(f->d_ctl + slot, &c, sizeof(DevCtl), cudaMemcpyHostToDevice, f->stream));
     int r = encode_maps(f, slot);
+    if (r == HC_OK && has_fixed(S))
+        find_aux(f->sch.precision, S.dim)->fixed_ghosts(f->d_inst, slot, f->plan[0].n_state_bufs, f->stream);
     if (r == HC_OK && host) r = set_state(f, slot, host, layout, 1, true);
     if (r == HC_OK && !host && init) r = init_state(f, slot, *init, true);
     if (r != HC_OK) {

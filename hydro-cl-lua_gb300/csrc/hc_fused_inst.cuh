@@ -223,6 +223,9 @@ void add_aux(std::vector<AuxLauncher>& v) {
     a.sums = [](const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s) {
         k_sums<T, DIM><<<blocks, 256, 0, s>>>(inst, slot, buf, vol, partial);
     };
+    a.fixed_ghosts = [](const DevInst* inst, int slot, int nbufs, cudaStream_t s) {
+        k_fixed_ghosts<T, DIM><<<64, 256, 0, s>>>(inst, slot, nbufs);
+    };
     a.slab = [](const DevInst* inst, int slot, int buf, int axis, int side, int dir, double* staging, long long cells,
                 cudaStream_t s) {
         k_slab<T, DIM><<<gridFor(cells), 256, 0, s>>>(inst, slot, buf, axis, side, dir, staging);

@@ -90,6 +90,9 @@ struct PlainParams {
     double gamma, rhoMin, PMin;
     int flux;             // HC_FLUX_*
     int hllcMethod;       // euler-hllc's hllcMethod, 0..2
+    int entropyFix;       // Roe: useEntropyFluxFix, with its factor
+    double entropyFactor;
+    double fixedCons[6][5];   // HC_BOUNDARY_FIXED sides
 };
 
 struct PlainSolver;   // defined in hc_plain.cu

@@ -121,6 +121,7 @@ struct Eos {
     int hllcMethod;   // euler-hllc's hllcMethod, 0..2
     float invg1;      // 1 / (gamma - 1)
     int recon;        // HC_RECON_*
+    float entropyFactor;   // the Roe flux's entropy fix factor, 0: off
 };
 
 // A conserved state in the interface frame: rho, m_n, m_t1, m_t2, ETotal.
@@ -367,9 +368,22 @@ __device__ __forceinline__ void hll(V* F, const Eos& s, const C5<V>& UL, const C
     }
 }
 
+// |lambda| of a Roe wave after useEntropyFluxFix (roe.cl:83-101): where
+// |lambda| < dws = factor Cs, |sign(lambda) (lambda^2 / dws + dws) / 2|, with
+// OpenCL's sign(0) = 0 keeping a zero speed zero; |lambda| itself with the
+// fix off (factor 0: nothing is below dws = 0).
+template <typename V>
+__device__ __forceinline__ V fixedAbs(V lambda, V Cs, float factor) {
+    V const a = absv(lambda), zero = splat<V>(0.f);
+    V const dws = mul(splat<V>(factor), Cs);
+    V const fixd = mul(splat<V>(.5f), add(mul(mul(lambda, lambda), rcp(dws)), dws));
+    return sel(lt(a, dws), sel(le(a, zero), zero, fixd), a);
+}
+
 // Roe flux without a flux limiter (roe.cl:17-163) in the fluxFromCons form
 // Euler inherits (roeUseFluxFromCons, eqn.lua:46):
-//   F = (F(UL) + F(UR)) / 2 - R |Lambda| L.(UR - UL) / 2.
+//   F = (F(UL) + F(UR)) / 2 - R |Lambda| L.(UR - UL) / 2
+// (|Lambda| after the entropy fix where it is on).
 template <typename V>
 __device__ __forceinline__ void roeCentral(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
     Eig<V> e;
@@ -379,9 +393,9 @@ __device__ __forceinline__ void roeCentral(V* F, const Eos& s, const C5<V>& UL, 
     for (int j = 0; j < 5; ++j) dU[j] = sub(UR.u[j], UL.u[j]);
     left(dW, e, s, dU);
     V const nh = splat<V>(-.5f);
-    V const c0 = mul(nh, absv(sub(e.vn, e.Cs)));
-    V const c1 = mul(nh, absv(e.vn));
-    V const c4 = mul(nh, absv(add(e.vn, e.Cs)));
+    V const c0 = mul(nh, fixedAbs(sub(e.vn, e.Cs), e.Cs, s.entropyFactor));
+    V const c1 = mul(nh, fixedAbs(e.vn, e.Cs, s.entropyFactor));
+    V const c4 = mul(nh, fixedAbs(add(e.vn, e.Cs), e.Cs, s.entropyFactor));
     fe[0] = mul(c0, dW[0]);
     fe[1] = mul(c1, dW[1]);
     fe[2] = mul(c1, dW[2]);
@@ -401,7 +415,8 @@ __device__ __forceinline__ void roeCentral(V* F, const Eos& s, const C5<V>& UL, 
 // Roe matrix has property U, F(UR) - F(UL) = R Lambda L.(UR - UL), and the
 // flux above equals the upwind form F(UL) + R min(Lambda, 0) L.(UR - UL):
 // one physical flux instead of two, built from the left side's pressure and
-// 1/rho that the average already has.  Other states take the form above.
+// 1/rho that the average already has.  Other states, and every state with the
+// entropy fix on (it changes |Lambda| but not Lambda), take the form above.
 template <typename V>
 __device__ __forceinline__ void roe(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
     if constexpr (nlanes<V>() == 1) {
@@ -411,15 +426,15 @@ __device__ __forceinline__ void roe(V* F, const Eos& s, const C5<V>& UL, const C
         bool low = false;
         float const rho = (lv || rv) ? eigenVac(e, s, UL, UR, lv, rv) : eigenRoe(e, s, UL, UR, PL, invL, low);
         finishEig(e, s, rho);
-        bool const pu = !(lv || rv || low || e.ident);
+        bool const pu = !(lv || rv || low || e.ident) && s.entropyFactor == 0.f;
         float dU[5], dW[5], fe[5];
 #pragma unroll
         for (int j = 0; j < 5; ++j) dU[j] = sub(UR.u[j], UL.u[j]);
         left(dW, e, s, dU);
         float const l0 = sub(e.vn, e.Cs), l4 = add(e.vn, e.Cs);
-        float const c0 = pu ? vmin(l0, 0.f) : mul(-.5f, absv(l0));
-        float const c1 = pu ? vmin(e.vn, 0.f) : mul(-.5f, absv(e.vn));
-        float const c4 = pu ? vmin(l4, 0.f) : mul(-.5f, absv(l4));
+        float const c0 = pu ? vmin(l0, 0.f) : mul(-.5f, fixedAbs(l0, e.Cs, s.entropyFactor));
+        float const c1 = pu ? vmin(e.vn, 0.f) : mul(-.5f, fixedAbs(e.vn, e.Cs, s.entropyFactor));
+        float const c4 = pu ? vmin(l4, 0.f) : mul(-.5f, fixedAbs(l4, e.Cs, s.entropyFactor));
         fe[0] = mul(c0, dW[0]);
         fe[1] = mul(c1, dW[1]);
         fe[2] = mul(c1, dW[2]);
@@ -450,10 +465,11 @@ __device__ __forceinline__ void roe(V* F, const Eos& s, const C5<V>& UL, const C
 // L.(UR - UL), operation for operation as roe<float> evaluates it where the
 // Roe average is the plain one.  Returns whether every lane has the plain
 // average (no vacuum side, enthalpy above its floor, averaged density at
-// least rhoMin); where a lane has not, F is not that lane's flux and the
-// caller evaluates roe<float> for it.
+// least rhoMin) and the entropy fix is off; where a lane has not, F is not
+// that lane's flux and the caller evaluates roe<float> for it.
 template <typename V>
 __device__ __forceinline__ bool roeUp(V* F, const Eos& s, const C5<V>& UL, const C5<V>& UR) {
+    if (s.entropyFactor != 0.f) return false;   // the entropy fix: roe<float> evaluates every face
     Mask<V> const lv = lt(UL.u[0], splat<V>(1e-5f)), rv = lt(UR.u[0], splat<V>(1e-5f));
     Eig<V> e;
     V PL, invL;

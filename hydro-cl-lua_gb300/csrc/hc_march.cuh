@@ -172,7 +172,8 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
 
         TileK<float> K;
         makeTileK<float>(K, I, ctl, &st, slopeLim, 0, HC_FLUX_ROE, 2, HC_RECON_PLM_CONS);
-        lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon};
+        lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon,
+                             (float)K.fe.entropyFactor};
         int const slim = SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter;
         float2 const area = make_float2(K.area[0], K.area[1]);
         bool const skipX = K.skip[0], skipY = K.skip[1], zeroX = K.zero[0], zeroY = K.zero[1];

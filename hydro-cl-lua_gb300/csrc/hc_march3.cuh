@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
 
         TileK<float> K;
         makeTileK<float>(K, I, ctl, &st, slopeLim, 0, HC_FLUX_ROE, 2, HC_RECON_PLM_CONS);
-        lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon};
+        lanes::Eos const le{K.fe.gamma, K.fe.g1, K.fe.rhoMin, K.fe.PMin, K.fe.hllcMethod, K.invg1, K.re.recon,
+                             (float)K.fe.entropyFactor};
         int const slim = SLOPE >= 0 ? SLOPE : K.fe.slopeLimiter;
         bool const skipX = K.skip[0], skipY = K.skip[1], skipZ = K.skip[2];
         bool const zeroX = K.zero[0], zeroY = K.zero[1], zeroZ = K.zero[2];

@@ -43,6 +43,8 @@ __device__ __forceinline__ Eos eosOf(const PlainParams& s) {
     e.flux = s.flux;
     e.hllcMethod = s.hllcMethod;
     e.recon = s.recon;
+    e.entropyFix = s.entropyFix;
+    e.entropyFactor = s.entropyFactor;
     return e;
 }
 
@@ -88,6 +90,12 @@ __global__ void k_boundary(PlainParams s, Cons* U, int side) {
             } else if (method == HC_BOUNDARY_FREEFLOW) {
                 if (mm == 0) { dst = j; src = kGhost; }
                 else { dst = gsSide - kGhost + j; src = gsSide - kGhost - 1; }
+            } else if (method == HC_BOUNDARY_FIXED) {
+                // gridsolver.lua:746-765: the side's constant state (ePot 0)
+                Cons& o = at(mm == 0 ? j : gsSide - kGhost + j);
+                for (int k = 0; k < 5; ++k) o.p[k] = s.fixedCons[2 * side + mm][k];
+                o.p[5] = 0.;
+                continue;
             } else if (method == HC_BOUNDARY_LINEAR || method == HC_BOUNDARY_QUADRATIC) {
                 // gridsolver.lua:783-858: outward, each ghost from the two
                 // (three) cells inside it, all 6 reals
@@ -375,6 +383,9 @@ int plain_create(const hc_solver_desc& d, cudaStream_t stream, PlainSolver** out
     p.gamma = d.gamma;
     p.rhoMin = d.rho_min;
     p.PMin = d.p_min;
+    p.entropyFix = d.entropy_fix != 0;
+    p.entropyFactor = d.entropy_fix_factor;
+    std::memcpy(p.fixedCons, d.fixed_cons, sizeof(p.fixedCons));
     s->stream = stream;
     s->order = rk_table(d.integrator).order;
     s->blocks = (p.numCells + kThreads - 1) / kThreads;
@@ -504,6 +515,7 @@ int plain_expand_full(const hc_solver_desc& d, const void* interior_dev, int lay
     p.stepsize[2] = p.gs[0] * p.gs[1];
     p.numCells = (long long)p.gs[0] * p.gs[1] * p.gs[2];
     for (int k = 0; k < 6; ++k) p.bc[k] = d.boundary[k];
+    std::memcpy(p.fixedCons, d.fixed_cons, sizeof(p.fixedCons));
     p.gamma = d.gamma;
     p.rhoMin = d.rho_min;
     p.PMin = d.p_min;

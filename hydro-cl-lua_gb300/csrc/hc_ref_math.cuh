@@ -26,6 +26,8 @@ struct Eos {
     int flux;   // HC_FLUX_*
     int hllcMethod;   // euler-hllc's hllcMethod, 0..2
     int recon;  // HC_RECON_*
+    int entropyFix;        // Roe: useEntropyFluxFix
+    double entropyFactor;  // its entropyFluxFixLimitingFactor
 };
 
 // OpenCL C max/min on floating types.
@@ -233,7 +235,16 @@ __device__ __forceinline__ void roeFlux(double* F, const Eos& s, const double* U
     double const v_n = C.eig.v[side];
     double fluxEig[5];
     for (int j = 0; j < 5; ++j) {
-        double const lambda = j == 0 ? v_n - Cs_nLen : (j == 4 ? v_n + Cs_nLen : v_n);
+        double lambda = j == 0 ? v_n - Cs_nLen : (j == 4 ? v_n + Cs_nLen : v_n);
+        if (s.entropyFix) {
+            // useEntropyFluxFix (roe.cl:83-101): Harten's fix of the wave
+            // speeds slower than factor * Cs; OpenCL's sign() keeps +-0
+            double const dws = s.entropyFactor * C.eig.Cs;
+            if (fabs(lambda) < dws) {
+                double const sg = lambda > 0 ? 1. : (lambda < 0 ? -1. : lambda);
+                lambda = sg * .5 * (lambda * lambda / dws + dws);
+            }
+        }
         fluxEig[j] = 0.;
         double const sgn = lambda >= 0 ? 1. : -1.;
         if (lim) {

@@ -41,7 +41,7 @@ INTEGRATORS = [
     "Runge-Kutta 3", "Runge-Kutta 4", "Runge-Kutta 4, 3/8ths rule", "Runge-Kutta 2, TVD",
     "Runge-Kutta 2, non-TVD", "Runge-Kutta 3, TVD", "Runge-Kutta 4, TVD", "Runge-Kutta 4, non-TVD",
 ]
-BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3, "linear": 4, "quadratic": 5}
+BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3, "linear": 4, "quadratic": 5, "fixed": 6}
 RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2, "plm prim": 3, "plm athena": 4}
 # hydro/flux/*.lua names
 FLUXES = ["roe", "hll", "rusanov", "euler-hllc"]
@@ -70,6 +70,8 @@ class SolverDesc(ctypes.Structure):
         ("gamma", ctypes.c_double), ("rho_min", ctypes.c_double), ("p_min", ctypes.c_double),
         ("cfl", ctypes.c_double), ("fixed_dt", ctypes.c_double),
         ("flux", ctypes.c_int), ("hllc_method", ctypes.c_int),
+        ("entropy_fix", ctypes.c_int), ("reserved0", ctypes.c_int), ("entropy_fix_factor", ctypes.c_double),
+        ("fixed_cons", (ctypes.c_double * 5) * 6),
     ]
 
 
@@ -339,9 +341,14 @@ def make_desc(args):
     bnd = args.get("boundary", {}) or {}
     if isinstance(bnd, str):
         bnd = {k: bnd for k in SIDES}
+    eq = args.get("eqnArgs", {}) or {}
     for k, side in enumerate(SIDES):
         name = bnd.get(side, "freeflow")
         if isinstance(name, dict):
+            # {"name": "fixed", "cons": [...]} or {"name": "fixed", "prim": {...}}
+            cons = fixed_cons(name, float(eq.get("heatCapacityRatio", 7.0 / 5.0)))
+            for f in range(5):
+                d.fixed_cons[k][f] = cons[f]
             name = name["name"]
         if name not in BOUNDARIES:
             raise ValueError("unknown boundary %r" % name)
@@ -363,7 +370,27 @@ def make_desc(args):
     d.p_min = float(eq.get("PMin", 1e-7))
     d.cfl = float(args.get("cfl", 0.5))
     d.fixed_dt = float(args.get("fixedDT", 0.0) or 0.0)
+    # the Roe flux's entropy fix (hydro/flux/roe.lua:10-16)
+    d.entropy_fix = 1 if args.get("useEntropyFluxFix", False) else 0
+    d.entropy_fix_factor = float(args.get("entropyFluxFixLimitingFactor", 0.2))
     return d
+
+
+def fixed_cons(spec, gamma):
+    """The constant ghost state of a 'fixed' boundary side (the reference's
+    BoundaryFixed takes generated fixedCode; here the state itself):
+    {"name": "fixed", "cons": [rho, m.x, m.y, m.z, ETotal]} or
+    {"name": "fixed", "prim": {"rho": r, "v": [vx, vy, vz], "P": p}} (consFromPrim)."""
+    if spec.get("name") != "fixed":
+        return [0.0] * 5
+    if "cons" in spec:
+        c = [float(x) for x in spec["cons"]]
+        if len(c) != 5:
+            raise ValueError("a fixed boundary's cons has 5 values")
+        return c
+    w = spec["prim"]
+    v = [float(x) for x in list(w.get("v", [0, 0, 0])) + [0.0] * 3][:3]
+    return [float(x) for x in cons_from_prim(float(w["rho"]), v[0], v[1], v[2], float(w["P"]), gamma)[0, :5]]
 
 
 def interior_count(desc):

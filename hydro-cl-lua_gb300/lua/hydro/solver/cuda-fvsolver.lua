@@ -46,8 +46,17 @@ local function descFromSolver(self, args)
 	local k = 0
 	for _,xi in ipairs{'x','y','z'} do
 		for _,mm in ipairs{'min','max'} do
-			d.boundary[k] = assert(hc.boundaryIndex[self.boundaryMethods[xi..mm].name],
-				"the cuda solver provides none, periodic, mirror, freeflow, linear and quadratic boundaries")
+			local name = self.boundaryMethods[xi..mm].name
+			d.boundary[k] = assert(hc.boundaryIndex[name],
+				"the cuda solver provides none, periodic, mirror, freeflow, linear, quadratic and fixed boundaries")
+			if name == 'fixed' then
+				-- BoundaryFixed's fixedCode generates OpenCL; the library takes
+				-- the constant state itself: args.cudaFixedCons[side] =
+				-- {rho, m.x, m.y, m.z, ETotal}
+				local c = assert((args.cudaFixedCons or {})[xi..mm],
+					"a fixed boundary needs cudaFixedCons."..xi..mm.." = {rho, m.x, m.y, m.z, ETotal}")
+				for f=0,4 do d.fixed_cons[k][f] = c[f+1] end
+			end
 			k = k + 1
 		end
 	end
@@ -64,6 +73,9 @@ local function descFromSolver(self, args)
 	d.fixed_dt = self.useFixedDT and self.fixedDT or 0
 	d.flux = flux
 	d.hllc_method = self.flux.hllcMethod and (self.flux.hllcMethod + 1) or 0
+	-- Roe's useEntropyFluxFix (hydro/flux/roe.lua:10-16)
+	d.entropy_fix = self.flux.useEntropyFluxFix and 1 or 0
+	d.entropy_fix_factor = self.flux.entropyFluxFixLimitingFactor or .2
 	return d
 end
 

@@ -28,6 +28,10 @@ typedef struct hc_solver_desc {
 	double fixed_dt;
 	int flux;
 	int hllc_method;
+	int entropy_fix;
+	int reserved0;
+	double entropy_fix_factor;
+	double fixed_cons[6][5];
 } hc_solver_desc;
 typedef struct hc_context hc_context;
 typedef struct hc_solver hc_solver;
@@ -137,7 +141,7 @@ for i, name in ipairs{
 	'Runge-Kutta 3, TVD', 'Runge-Kutta 4, TVD', 'Runge-Kutta 4, non-TVD',
 } do M.integratorIndex[name] = i - 1 end
 
-M.boundaryIndex = {none = 0, periodic = 1, mirror = 2, freeflow = 3, linear = 4, quadratic = 5}
+M.boundaryIndex = {none = 0, periodic = 1, mirror = 2, freeflow = 3, linear = 4, quadratic = 5, fixed = 6}
 M.fluxIndex = {roe = 0, hll = 1, rusanov = 2, ['euler-hllc'] = 3}
 M.reconIndex = {['piecewise constant'] = 1, ['plm cons'] = 2, ['plm prim'] = 3, ['plm athena'] = 4}
 M.precisionIndex = {['f64 plain'] = 0, f64 = 1, f32 = 2}

@@ -54,16 +54,19 @@ extern "C" {
 #define HC_ERR_TIMEOUT     -7   /* a bounded device wait ran out */
 #define HC_ERR_STATE       -8   /* call not valid in the handle's current state */
 
-/* boundary names (gridsolver.lua:617-860); "fixed" needs the initial
- * condition's generated fixedCode and the sphere / cylinder ones curvilinear
- * coordinates: not provided */
+/* boundary names (gridsolver.lua:617-860); the sphere / cylinder ones need
+ * curvilinear coordinates: not provided */
 #define HC_BOUNDARY_NONE      0
 #define HC_BOUNDARY_PERIODIC  1
 #define HC_BOUNDARY_MIRROR    2
 #define HC_BOUNDARY_FREEFLOW  3
 #define HC_BOUNDARY_LINEAR    4   /* ghost = 2 U[i1] - U[i2], ghosts filled outward (gridsolver.lua:783-813) */
 #define HC_BOUNDARY_QUADRATIC 5   /* ghost = 3 U[i1] - 3 U[i2] + U[i3] (gridsolver.lua:815-858) */
-#define HC_NUM_BOUNDARIES     6
+#define HC_BOUNDARY_FIXED     6   /* Dirichlet: every ghost cell of the side holds the constant state
+                                     fixed_cons (BoundaryFixed, gridsolver.lua:746-765, whose fixedCode
+                                     writes one constant cons_t, as the square cavity's does,
+                                     hydro/init/euler.lua:1856-1875) */
+#define HC_NUM_BOUNDARIES     7
 
 /* limiter table, in the order of hydro/app.lua:614-635 (reference index - 1);
  * HC_LIMITER_DONOR_CELL as flux limiter means "no flux limiter" */
@@ -164,6 +167,15 @@ typedef struct hc_solver_desc {
     double fixed_dt;         /* > 0: useFixedDT with this dt; <= 0: CFL dt */
     int    flux;             /* HC_FLUX_* (0 = roe) */
     int    hllc_method;      /* HC_HLLC_* (euler-hllc only) */
+    /* Roe only: useEntropyFluxFix (hydro/flux/roe.lua:10-16, roe.cl:83-101),
+     * off by default: where |lambda| < factor * Cs, lambda becomes
+     * sign(lambda) (lambda^2 / (factor Cs) + factor Cs) / 2 */
+    int    entropy_fix;      /* 0: off, 1: on */
+    int    reserved0;
+    double entropy_fix_factor;   /* entropyFluxFixLimitingFactor; the reference's default is .2 */
+    /* the ghost cells' conserved state (rho, m.x, m.y, m.z, ETotal) of each
+     * side whose boundary is HC_BOUNDARY_FIXED, in boundary[]'s order (ePot 0) */
+    double fixed_cons[6][5];
 } hc_solver_desc;
 
 /* Initial conditions generated on the device (the reference builds every

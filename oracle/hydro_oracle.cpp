@@ -47,7 +47,7 @@ struct prim_t { real rho; real v[3]; real P; real ePot; };
 // hydro/eqn/euler.lua:298-307 -- eigen_t
 struct eigen_t { real rho; real v[3]; real hTotal; real Cs; real vSq; real vL[3]; };
 
-enum { BC_NONE = 0, BC_PERIODIC = 1, BC_MIRROR = 2, BC_FREEFLOW = 3, BC_LINEAR = 4, BC_QUADRATIC = 5 };
+enum { BC_NONE = 0, BC_PERIODIC = 1, BC_MIRROR = 2, BC_FREEFLOW = 3, BC_LINEAR = 4, BC_QUADRATIC = 5, BC_FIXED = 6 };
 enum { RECON_NONE = 0, RECON_PIECEWISE_CONSTANT = 1, RECON_PLM_CONS = 2, RECON_PLM_PRIM = 3, RECON_PLM_ATHENA = 4 };
 enum { FLUX_ROE = 0, FLUX_HLL = 1, FLUX_RUSANOV = 2, FLUX_HLLC = 3 };
 
@@ -121,6 +121,9 @@ struct Solver {
 	int fluxType;      // FLUX_*
 	int hllcMethod;    // euler-hllc's hllcMethod: 0, 1, 2
 	real gamma, rhoMin, PMin, cfl, fixedDT;
+	bool entropyFix;   // Roe: useEntropyFluxFix
+	real entropyFactor;   // entropyFluxFixLimitingFactor
+	real fixedCons[6][5];  // BC_FIXED sides: the ghost cells' state
 	static const int numGhost = 2;
 
 	// state
@@ -323,10 +326,16 @@ static void fluxFromCons(cons_t& F, const Solver& s, const cons_t& U, int side) 
 	F.ptr[5] = 0;
 }
 
-// hydro/flux/roe.cl:17-163, entropy fix off, with roeUseFluxFromCons: Euler
-// does not set it and inherits Equation.roeUseFluxFromCons = true
-// (hydro/eqn/eqn.lua:46), so the flux is R.fluxEig + (F(UL) + F(UR)) / 2 with
-// fluxEig_j = 0 - lambda_j dW_j (sgn + phi (lambda_j dt/dx - sgn)) / 2.
+// OpenCL C sign(): 1 for x > 0, -1 for x < 0, x itself for +-0, 0 for NaN.
+static inline real clSign(real x) { return x > 0 ? 1. : (x < 0 ? -1. : (x == 0 ? x : 0.)); }
+
+// hydro/flux/roe.cl:17-163 with roeUseFluxFromCons: Euler does not set it and
+// inherits Equation.roeUseFluxFromCons = true (hydro/eqn/eqn.lua:46), so the
+// flux is R.fluxEig + (F(UL) + F(UR)) / 2 with
+// fluxEig_j = 0 - lambda_j dW_j (sgn + phi (lambda_j dt/dx - sgn)) / 2.  With
+// useEntropyFluxFix (roe.cl:83-101) each lambda_j with |lambda_j| < factor Cs
+// is first replaced by sign(lambda_j) (lambda_j^2 / dws + dws) / 2, dws =
+// factor Cs; sgn and the flux limiter's ratio then follow the new value.
 static void roeFluxForInterface(
 	cons_t& resultFlux, const Solver& s,
 	const cons_t& UL, const cons_t& UR, int side, bool useFluxLimiter, real dt_dx,
@@ -357,8 +366,13 @@ static void roeFluxForInterface(
 		eigen_leftTransform(deltaUEigR, s, eigR, deltaUR, side);
 	}
 
+	real const speedOfSound = eig.Cs;
 	for (int j = 0; j < 5; ++j) {
-		real const lambda = j == 0 ? v_n - Cs_nLen : (j == 4 ? v_n + Cs_nLen : v_n);
+		real lambda = j == 0 ? v_n - Cs_nLen : (j == 4 ? v_n + Cs_nLen : v_n);
+		if (s.entropyFix) {
+			real const dws = s.entropyFactor * speedOfSound;
+			if (fabs(lambda) < dws) lambda = clSign(lambda) * .5 * (lambda * lambda / dws + dws);
+		}
 		fluxEig[j] = 0.;
 		real const sgnLambda = lambda >= 0 ? 1 : -1;
 		if (useFluxLimiter) {
@@ -593,6 +607,13 @@ static void boundary(Solver& s) {
 					} else if (method == BC_FREEFLOW) {
 						if (mm == 0) { dst = j; src = G; }
 						else { dst = gsSide - G + j; src = gsSide - G - 1; }
+					} else if (method == BC_FIXED) {
+						// gridsolver.lua:746-765: the side's ghosts take the
+						// constant state fixedCode writes (consFromPrim, ePot 0)
+						cons_t& d = at(mm == 0 ? j : gsSide - G + j);
+						for (int k = 0; k < 5; ++k) d.ptr[k] = s.fixedCons[2 * side + mm][k];
+						d.ptr[5] = 0.;
+						continue;
 					} else if (method == BC_LINEAR || method == BC_QUADRATIC) {
 						// gridsolver.lua:783-858: outward from the interior, each
 						// ghost from the two (three) cells inside it, all 6 reals
@@ -631,9 +652,6 @@ static void constrainU(Solver& s) {
 	});
 	boundary(s);
 }
-
-// OpenCL C sign(): 1 for x > 0, -1 for x < 0, x itself for +-0, 0 for NaN.
-static inline real clSign(real x) { return x > 0 ? 1. : (x < 0 ? -1. : (x == 0 ? x : 0.)); }
 
 static inline real& primAt(prim_t& W, int j) { return j == 0 ? W.rho : (j < 4 ? W.v[j - 1] : (j == 4 ? W.P : W.ePot)); }
 
@@ -993,6 +1011,10 @@ typedef struct or_desc {
 	double fixed_dt;
 	int flux;          // FLUX_*: roe, hll, rusanov, euler-hllc
 	int hllc_method;   // 0: the reference's default (its hllcMethod 2); 1, 2, 3: its hllcMethod 0, 1, 2
+	int entropy_fix;   // Roe: useEntropyFluxFix
+	int reserved0;
+	double entropy_fix_factor;
+	double fixed_cons[6][5];   // BC_FIXED sides
 } or_desc;
 
 void* or_create(const or_desc* d) {
@@ -1022,6 +1044,10 @@ void* or_create(const or_desc* d) {
 	s->PMin = d->p_min;
 	s->cfl = d->cfl;
 	s->fixedDT = d->fixed_dt;
+	s->entropyFix = d->entropy_fix != 0;
+	s->entropyFactor = d->entropy_fix_factor;
+	for (int k = 0; k < 6; ++k)
+		for (int f = 0; f < 5; ++f) s->fixedCons[k][f] = d->fixed_cons[k][f];
 	s->t = 0;
 	s->U.assign(s->numCells, cons_t{});
 	s->ULR.assign(2 * s->numCells * s->dim, cons_t{});

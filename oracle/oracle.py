@@ -42,7 +42,7 @@ INTEGRATORS = [
     "Runge-Kutta 2, non-TVD", "Runge-Kutta 3, TVD", "Runge-Kutta 4, TVD",
     "Runge-Kutta 4, non-TVD",
 ]
-BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3, "linear": 4, "quadratic": 5}
+BOUNDARIES = {"none": 0, "periodic": 1, "mirror": 2, "freeflow": 3, "linear": 4, "quadratic": 5, "fixed": 6}
 RECONS = {None: 0, False: 0, "piecewise constant": 1, "plm cons": 2, "plm prim": 3, "plm athena": 4}
 
 
@@ -85,6 +85,10 @@ class OrDesc(ctypes.Structure):
         ("fixed_dt", ctypes.c_double),
         ("flux", ctypes.c_int),
         ("hllc_method", ctypes.c_int),
+        ("entropy_fix", ctypes.c_int),
+        ("reserved0", ctypes.c_int),
+        ("entropy_fix_factor", ctypes.c_double),
+        ("fixed_cons", (ctypes.c_double * 5) * 6),
     ]
 
 # flux names in the reference's vocabulary (hydro/flux/*.lua)
@@ -152,8 +156,16 @@ def make_desc(cfg):
     bnd = cfg.get("boundary", {}) or {}
     if isinstance(bnd, str):
         bnd = {k: bnd for k in ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")}
+    eq = cfg.get("eqnArgs", {}) or {}
+    gamma = float(eq.get("heatCapacityRatio", 7.0 / 5.0))
     for k, name in enumerate(("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")):
-        d.boundary[k] = BOUNDARIES[bnd.get(name, "freeflow")]
+        spec = bnd.get(name, "freeflow")
+        if isinstance(spec, dict):
+            cons = fixed_cons(spec, gamma)
+            for f in range(5):
+                d.fixed_cons[k][f] = cons[f]
+            spec = spec["name"]
+        d.boundary[k] = BOUNDARIES[spec]
     d.flux_limiter = LIMITERS.index(cfg.get("fluxLimiter", "donor cell"))
     d.recon = RECONS[cfg.get("usePLM", None)]
     d.slope_limiter = LIMITERS.index(cfg.get("slopeLimiter", "donor cell"))
@@ -167,7 +179,25 @@ def make_desc(cfg):
     d.flux = FLUXES.index(cfg.get("flux", "roe"))
     # euler-hllc's hllcMethod (default 2, euler-hllc.lua:19); 0 in the descriptor is that default
     d.hllc_method = int(cfg["hllcMethod"]) + 1 if "hllcMethod" in cfg else 0
+    # hydro/flux/roe.lua:10-16
+    d.entropy_fix = 1 if cfg.get("useEntropyFluxFix", False) else 0
+    d.entropy_fix_factor = float(cfg.get("entropyFluxFixLimitingFactor", 0.2))
     return d
+
+
+def fixed_cons(spec, gamma):
+    """The constant state of a 'fixed' boundary side, {"name": "fixed", "cons":
+    [rho, m.x, m.y, m.z, ETotal]} or {"name": "fixed", "prim": {"rho", "v",
+    "P"}} (consFromPrim, hydro/eqn/euler.cl:163-173, ePot 0)."""
+    if spec.get("name") != "fixed":
+        return [0.0] * 5
+    if "cons" in spec:
+        return [float(c) for c in spec["cons"]]
+    w = spec["prim"]
+    rho, P = float(w["rho"]), float(w["P"])
+    v = [float(c) for c in list(w.get("v", [0, 0, 0])) + [0.0] * 3][:3]
+    return [rho, v[0] * rho, v[1] * rho, v[2] * rho,
+            rho * (.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2])) + P / (gamma - 1.)]
 
 
 class OracleSolver:

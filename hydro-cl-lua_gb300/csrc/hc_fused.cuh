@@ -794,8 +794,10 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
             if (DIM == 1) tma_load<2>(box, map, x0, 0, 0, 0, bar);
             else if (DIM == 2) tma_load<3>(box, map, x0, y0, 0, 0, bar);
             else tma_load<4>(box, map, x0, y0, z0, 0, bar);
-            // the other RK states this tile's cells combine (read from global
-            // memory by the epilogue) into L2 while the sweeps run
+            // the first other RK state this tile's cells combine (read from
+            // global memory by the epilogue) into L2 while the sweeps run; one
+            // tensor prefetch per state would put up to three back to back
+            // (RK4-TVD), a pattern under which an earlier kernel faulted
 #pragma unroll
             for (int m = 0; m < 4; ++m) {
                 if (m >= st.n_alpha) break;
@@ -805,6 +807,7 @@ __global__ void __launch_bounds__(NT, OCC) k_stage(const __grid_constant__ Stage
                 if (DIM == 1) tma_prefetch_l2<2>(amap, x0, 0, 0, 0);
                 else if (DIM == 2) tma_prefetch_l2<3>(amap, x0, y0, 0, 0);
                 else tma_prefetch_l2<4>(amap, x0, y0, z0, 0);
+                break;
             }
             // the box of this CTA's next item into L2 while this one is computed
             int const next = item + (int)gridDim.x;

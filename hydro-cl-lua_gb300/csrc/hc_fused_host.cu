@@ -980,6 +980,7 @@ int fused_stats(FusedSet* f, hc_batch_stats* st) {
         st->tile[d][1] = f->launcher[d] ? f->launcher[d]->ty : 0;
         st->tile[d][2] = f->launcher[d] ? f->launcher[d]->tz : 0;
         st->schedule[d] = f->launcher[d] ? f->launcher[d]->variant : 0;
+        st->marching[d] = f->launcher[d] ? f->launcher[d]->march : 0;
     }
     return HC_OK;
 }

@@ -91,7 +91,7 @@ class Done(ctypes.Structure):
 class BatchStats(ctypes.Structure):
     _fields_ = [("active", ctypes.c_int), ("occupied", ctypes.c_int), ("bytes_in_use", ctypes.c_size_t),
                 ("tiles", ctypes.c_longlong), ("cells", ctypes.c_longlong), ("n_stages", ctypes.c_int),
-                ("tile", (ctypes.c_int * 3) * 3), ("schedule", ctypes.c_int * 3)]
+                ("tile", (ctypes.c_int * 3) * 3), ("schedule", ctypes.c_int * 3), ("marching", ctypes.c_int * 3)]
 
 
 class Init(ctypes.Structure):
@@ -768,7 +768,8 @@ class Batch:
         s = BatchStats()
         _check(self.L.hc_batch_stats_get(self.h, ctypes.byref(s)))
         return dict(active=s.active, occupied=s.occupied, bytes_in_use=s.bytes_in_use, tiles=s.tiles, cells=s.cells,
-                    n_stages=s.n_stages, tile=[list(s.tile[d]) for d in range(3)], schedule=list(s.schedule))
+                    n_stages=s.n_stages, tile=[list(s.tile[d]) for d in range(3)], schedule=list(s.schedule),
+                    marching=[bool(m) for m in s.marching])
 
     def conservation(self, slot):
         s = (ctypes.c_double * 5)()

@@ -323,6 +323,8 @@ typedef struct hc_batch_stats {
     int       n_stages;          /* stage launches per update and dimension */
     int       tile[3][3];        /* tile shape (x, y, z) in use per dimension 1..3 */
     int       schedule[3];       /* stage-kernel schedule in use per dimension (hc_batch_set_schedule's variant) */
+    int       marching[3];       /* 1: that schedule's kernel marches strips (2D) or tiles (3D) along the
+                                    grid instead of loading tiles */
 } hc_batch_stats;
 
 int hc_batch_create(hc_context* ctx, const hc_batch_desc* desc, hc_batch** out);

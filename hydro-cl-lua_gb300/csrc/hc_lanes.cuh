@@ -258,7 +258,7 @@ __device__ __forceinline__ void identLanes(V* out, const Eig<V>& e, const V* X) 
 //   q = (g-1)(X0 vSq/2 - X_m.v + X4), k = Cs (X0 vn - Xn),
 //   w = ((q+k)/(2Cs^2), X0 - 2q/(2Cs^2), Xt1 - X0 vt1, Xt2 - X0 vt2, (q-k)/(2Cs^2))
 // evaluated as q = (g-1)(X0 |v|^2/2 + (X4 - X_m.v)), k' = Xn - X0 vn = -k/Cs.
-template <typename V>
+template <typename V, bool IDENT = true>
 __device__ __forceinline__ void left(V* w, const Eig<V>& e, const Eos& s, const V* X) {
     V const mv = fma(X[3], e.vt2, fma(X[2], e.vt1, mul(X[1], e.vn)));
     V const q = mul(splat<V>(s.g1), fma(X[0], e.hvSq, sub(X[4], mv)));
@@ -269,13 +269,13 @@ __device__ __forceinline__ void left(V* w, const Eig<V>& e, const Eos& s, const 
     w[2] = fma(nX0, e.vt1, X[2]);
     w[3] = fma(nX0, e.vt2, X[3]);
     w[4] = mul(fma(e.Cs, kp, q), e.invD);
-    identLanes(w, e, X);
+    if constexpr (IDENT) identLanes(w, e, X);
 }
 
 // eigen_rightTransform (euler.cl:493-542) in the interface frame:
 //   S = W0 + W1 + W4, D = W4 - W0,
 //   F = (S, S vn + Cs D, S vt1 + W2, S vt2 + W3, hT (W0 + W4) + Cs vn D + vSq W1 / 2 + vt1 W2 + vt2 W3)
-template <typename V>
+template <typename V, bool IDENT = true>
 __device__ __forceinline__ void right(V* F, const Eig<V>& e, const V* W) {
     V const S = add(add(W[0], W[1]), W[4]);
     V const D = sub(W[4], W[0]);
@@ -293,7 +293,7 @@ __device__ __forceinline__ void right(V* F, const Eig<V>& e, const V* W) {
     F[2] = f2;
     F[3] = f3;
     F[4] = f4;
-    identLanes(F, e, W);
+    if constexpr (IDENT) identLanes(F, e, W);
 }
 
 // fluxFromCons (euler.cl:271-291) in the interface frame:
@@ -479,7 +479,7 @@ __device__ __forceinline__ bool roeUp(V* F, const Eos& s, const C5<V>& UL, const
     V dU[5], dW[5], fe[5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) dU[j] = sub(UR.u[j], UL.u[j]);
-    left(dW, e, s, dU);
+    left<V, false>(dW, e, s, dU);   // an identity lane is not plain: no lane select
     V const zero = splat<V>(0.f);
     V const c0 = vmin(sub(e.vn, e.Cs), zero);
     V const c1 = vmin(e.vn, zero);
@@ -489,7 +489,7 @@ __device__ __forceinline__ bool roeUp(V* F, const Eos& s, const C5<V>& UL, const
     fe[2] = mul(c1, dW[2]);
     fe[3] = mul(c1, dW[3]);
     fe[4] = mul(c4, dW[4]);
-    right(F, e, fe);
+    right<V, false>(F, e, fe);
     V const vn = mul(UL.u[1], invL);
     F[0] = add(F[0], UL.u[1]);
     F[1] = add(F[1], fma(UL.u[1], vn, PL));
@@ -771,6 +771,15 @@ __device__ __forceinline__ void constrain(V* u, const Eos& s, float invg1) {
     u[4] = sel(fix, fma(P, splat<V>(invg1), mul(rho, mul(splat<V>(.5f), vsq))), u[4]);
 }
 
+// For callers where every lane of the warp takes part (the marching
+// kernels' epilogues): constrain() with the clamp taken only when a lane
+// needs it (a warp-uniform test), then, when `last`, the cell's CFL dt.  An
+// unclamped lane's state is unchanged, so its 1/rho, |m|^2 and P are the values
+// dtCell would compute from it, and are reused; a warp with a clamped lane
+// evaluates dtCell.  The same bits as constrain() followed by dtCell().
+template <int DIM>
+__device__ __forceinline__ float constrainDtWarp(float* u, const Eos& s, float invg1, bool last, const float* gdx);
+
 // calcDTCell (calcDT.cl:38-73): min over the active sides of
 // dx / max(|vn - Cs|, |vn + Cs|, 1e-9), with Cs = 0 where P <= PMin and
 // infinite where rho < rhoMin.
@@ -791,6 +800,34 @@ __device__ __forceinline__ V dtCell(const V* u, const Eos& s, const float* gdx) 
         V a = vmax(absv(sub(vn, Cs)), absv(add(vn, Cs)));
         a = vmax(splat<V>(1e-9f), a);
         dt = vmin(dt, mul(splat<V>(gdx[side]), rcp(a)));
+    }
+    return dt;
+}
+
+template <int DIM>
+__device__ __forceinline__ float constrainDtWarp(float* u, const Eos& s, float invg1, bool last, const float* gdx) {
+    float const inf = __int_as_float(0x7f800000);
+    // below rhoMin, or NaN (max() would hide it in 1/rho)
+    bool const thin = !(u[0] >= s.rhoMin);
+    float const rho = vmax(u[0], s.rhoMin);
+    float const inv = rcp(rho);
+    float const m2 = fma(u[3], u[3], fma(u[2], u[2], mul(u[1], u[1])));
+    float const P0 = mul(s.g1, fma(mul(-.5f, m2), inv, u[4]));
+    bool const low = lt(P0, s.PMin);
+    if (__any_sync(0xffffffffu, thin || low)) {
+        constrain<float>(u, s, invg1);
+        return last ? dtCell<float, DIM>(u, s, gdx) : inf;
+    }
+    if (!last) return inf;
+    float Cs = sqr(mul(mul(s.gamma, P0), inv));
+    Cs = sel(le(P0, s.PMin), 0.f, Cs);
+    float dt = inf;
+#pragma unroll
+    for (int side = 0; side < DIM; ++side) {
+        float const vn = mul(u[1 + side], inv);
+        float a = vmax(absv(sub(vn, Cs)), absv(add(vn, Cs)));
+        a = vmax(1e-9f, a);
+        dt = vmin(dt, mul(gdx[side], rcp(a)));
     }
     return dt;
 }

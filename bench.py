@@ -389,9 +389,10 @@ def e2e_run(hc, ctx, work, inputs, cells, schedule, tick=8):
     run the configuration's 200 updates, reading every instance's status back
     (D2H) after each call of `tick` updates (the serving loop's tick), fetch
     every final state (D2H) into a second pinned buffer in one
-    hc_batch_fetch_many call.  Measured beside
-    it: the same job reading the status after every update, and with one
-    admit / fetch call per instance."""
+    hc_batch_fetch_many call (the library reads and writes page-locked
+    buffers in place over the host link).  The job runs three times and the
+    median is reported.  Measured beside it: the same job reading the status
+    after every update, and with one admit / fetch call per instance."""
     import ctypes
     nbytes = sum(u.nbytes for u in inputs)
     L = hc.load_library()
@@ -441,7 +442,11 @@ def e2e_run(hc, ctx, work, inputs, cells, schedule, tick=8):
         def run(per_call, many):
             return job(views, outs, per_call, many)
 
-        t0, t_admit, t_step, t1, evs, calls = run(tick, True)
+        # the job three times, the median by its total time reported (the
+        # first job of a process also pays the device's first allocations)
+        jobs = sorted((run(tick, True) for _ in range(3)), key=lambda j: j[3] - j[0])
+        t0, t_admit, t_step, t1, evs, calls = jobs[1]
+        job_s = [j[3] - j[0] for j in jobs]
         p0, _, _, p1, _, _ = run(1, True)
         q0, q_admit, q_step, q1, _, _ = run(tick, False)
     finally:
@@ -461,7 +466,9 @@ def e2e_run(hc, ctx, work, inputs, cells, schedule, tick=8):
             "value_status_every_update": cells * E2E_STEPS / (p1 - p0),
             "value_one_call_per_instance": cells * E2E_STEPS / (q1 - q0),
             "one_call_per_instance_seconds_admit": q_admit - q0, "one_call_per_instance_seconds_fetch": q1 - q_step,
-            "note": "whole job per call: admission (uploads, one admit_many call), 200 updates in calls of %d with "
+            "jobs_seconds": job_s,
+            "note": "median of 3 whole jobs (jobs_seconds: all three, sorted); each job: admission (uploads, one "
+                    "admit_many call; page-locked buffers read in place), 200 updates in calls of %d with "
                     "a status read after each call, result fetch (one fetch_many call); value_status_every_update: "
                     "the same job reading the status after every update; value_one_call_per_instance: one admit "
                     "and one fetch call per instance" % tick}

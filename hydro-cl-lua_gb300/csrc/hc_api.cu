@@ -609,30 +609,44 @@ int hc_batch_destroy(hc_batch* b) {
     return HC_OK;
 }
 
-static int batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout, const hc_init* init,
-                       double t_end, long long max_steps, unsigned long long tag, int* slot, int sync = 1) {
-    if (!b || !desc || !(cons || init) || !slot) return fail(HC_ERR_INVALID, "NULL argument");
+// The checks of an admission and the slot it would take (not yet marked).
+static int admit_check(hc_batch* b, const hc_solver_desc* desc, const hc_init* init, int layout, size_t extra_bytes,
+                       size_t* bytes, int* slot) {
     HC_CHECK(validate_desc(desc));
     if (init) HC_CHECK(init_validate(*init, *desc));
     if (desc->recon != b->d.recon || desc->slope_limiter != b->d.slope_limiter || desc->flux_limiter != b->d.flux_limiter ||
         desc->integrator != b->d.integrator || desc->flux != b->d.flux || desc->hllc_method != b->d.hllc_method)
         return fail(HC_ERR_INVALID, "the instance's scheme differs from the batch's");
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
-    if (max_steps <= 0) max_steps = LLONG_MAX;
-    HC_CHECK(use_device(b->ctx));
-    size_t const bytes = fused_instance_bytes(b->fused, *desc);
-    if (b->bytes_in_use + bytes > b->d.hbm_budget)
+    *bytes = fused_instance_bytes(b->fused, *desc);
+    if (b->bytes_in_use + extra_bytes + *bytes > b->d.hbm_budget)
         return fail(HC_ERR_BUDGET, "admission would exceed the batch's HBM budget");
     int s = -1;
     for (int k = 0; k < b->d.max_slots; ++k)
         if (!b->used[k]) { s = k; break; }
     if (s < 0) return fail(HC_ERR_NO_SLOT, "every slot is in use");
-    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps, 1, init, sync));
+    *slot = s;
+    return HC_OK;
+}
+
+static void admit_commit(hc_batch* b, int s, size_t bytes, unsigned long long tag) {
     b->used[s] = 1;
     b->reported[s] = 0;
     b->tags[s] = tag;
     b->slot_bytes[s] = bytes;
     b->bytes_in_use += bytes;
+}
+
+static int batch_admit(hc_batch* b, const hc_solver_desc* desc, const void* cons, int layout, const hc_init* init,
+                       double t_end, long long max_steps, unsigned long long tag, int* slot, int sync = 1) {
+    if (!b || !desc || !(cons || init) || !slot) return fail(HC_ERR_INVALID, "NULL argument");
+    if (max_steps <= 0) max_steps = LLONG_MAX;
+    HC_CHECK(use_device(b->ctx));
+    size_t bytes = 0;
+    int s = -1;
+    HC_CHECK(admit_check(b, desc, init, layout, 0, &bytes, &s));
+    HC_CHECK(fused_add(b->fused, s, *desc, cons, layout, t_end, max_steps, 1, init, sync));
+    admit_commit(b, s, bytes, tag);
     *slot = s;
     return HC_OK;
 }
@@ -659,16 +673,34 @@ int hc_batch_admit_many(hc_batch* b, int count, const hc_solver_desc* descs, con
     *n_admitted = 0;
     for (int k = 0; k < count; ++k) slots[k] = -1;
     HC_CHECK(use_device(b->ctx));
+    // every check first (slots taken in turn, the budget summed), then the
+    // accepted ones in one pass of the fused set
     int r = HC_OK;
-    for (int k = 0; k < count && r == HC_OK; ++k) {
-        if (!cons[k]) {
-            r = fail(HC_ERR_INVALID, "NULL argument");
-            break;
-        }
-        r = batch_admit(b, &descs[k], cons[k], layout, nullptr, t_end ? t_end[k] : INFINITY,
-                        max_steps ? max_steps[k] : 0, tags ? tags[k] : (unsigned long long)k, &slots[k], 0);
-        if (r == HC_OK) ++*n_admitted;
+    std::vector<size_t> bytes;
+    std::vector<double> te;
+    std::vector<long long> ms;
+    size_t extra = 0;
+    int n = 0;
+    for (; n < count; ++n) {
+        if (!cons[n]) { r = fail(HC_ERR_INVALID, "NULL argument"); break; }
+        size_t by = 0;
+        int s = -1;
+        r = admit_check(b, &descs[n], nullptr, layout, extra, &by, &s);
+        if (r != HC_OK) break;
+        b->used[s] = 1;   // taken for the following searches
+        slots[n] = s;
+        bytes.push_back(by);
+        extra += by;
+        te.push_back(t_end ? t_end[n] : INFINITY);
+        ms.push_back(max_steps && max_steps[n] > 0 ? max_steps[n] : LLONG_MAX);
     }
+    for (int k = 0; k < n; ++k) b->used[slots[k]] = 0;
+    int done = 0;
+    int ra = n ? fused_add_many(b->fused, n, slots, descs, cons, layout, te.data(), ms.data(), 1, &done) : HC_OK;
+    for (int k = 0; k < done; ++k) admit_commit(b, slots[k], bytes[k], tags ? tags[k] : (unsigned long long)k);
+    for (int k = done; k < count; ++k) slots[k] = -1;
+    *n_admitted = done;
+    if (ra != HC_OK && r == HC_OK) r = ra;
     // the host buffers are not read after return
     int const rs = fused_sync(b->fused);
     return r != HC_OK ? r : rs;
@@ -765,16 +797,12 @@ int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout) {
 int hc_batch_fetch_many(hc_batch* b, int count, const int* slots, void* const* cons, int layout) {
     if (!b || count < 0 || (count > 0 && (!slots || !cons))) return fail(HC_ERR_INVALID, "NULL argument");
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
-    size_t most = 0;
     for (int k = 0; k < count; ++k) {
         if (!cons[k]) return fail(HC_ERR_INVALID, "NULL argument");
         if (slots[k] < 0 || slots[k] >= b->d.max_slots || !b->used[slots[k]]) return fail(HC_ERR_STATE, "slot not in use");
-        most = std::max(most, fused_state_bytes(b->fused, slots[k], layout));
     }
     HC_CHECK(use_device(b->ctx));
-    HC_CHECK(fused_reserve_staging(b->fused, most));
-    int r = HC_OK;
-    for (int k = 0; k < count && r == HC_OK; ++k) r = fused_get_state(b->fused, slots[k], cons[k], layout, 0);
+    int const r = count ? fused_get_state_many(b->fused, count, slots, cons, layout) : HC_OK;
     int const rs = fused_sync(b->fused);
     return r != HC_OK ? r : rs;
 }

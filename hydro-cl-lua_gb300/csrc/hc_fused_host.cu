@@ -355,8 +355,9 @@ static int validate(const FusedSet* f, const hc_solver_desc& d) {
     return HC_OK;
 }
 
-// Tensor maps of a slot's state buffers for the launcher's box.
-static int encode_maps(FusedSet* f, int slot) {
+// Tensor maps of a slot's state buffers for the launcher's box (into the
+// pinned mirror; with `upload`, also to the device).
+static int encode_maps(FusedSet* f, int slot, bool upload = true) {
     Slot& S = f->slots[slot];
     const StageLauncher* L = f->launcher[S.dim - 1];
     const DevInst& I = S.inst;
@@ -388,8 +389,9 @@ static int encode_maps(FusedSet* f, int slot) {
                               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return fail(HC_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     }
-    HC_CUDA(cudaMemcpyAsync(f->d_tmaps + (size_t)slot * kMaxBufs, &f->h_tmaps[(size_t)slot * kMaxBufs],
-                            sizeof(CUtensorMap) * kMaxBufs, cudaMemcpyHostToDevice, f->stream));
+    if (upload)
+        HC_CUDA(cudaMemcpyAsync(f->d_tmaps + (size_t)slot * kMaxBufs, &f->h_tmaps[(size_t)slot * kMaxBufs],
+                                sizeof(CUtensorMap) * kMaxBufs, cudaMemcpyHostToDevice, f->stream));
     return HC_OK;
 }
 
@@ -508,8 +510,11 @@ size_t fused_state_bytes(const FusedSet* f, int slot, int layout) {
 
 int fused_reserve_staging(FusedSet* f, size_t bytes) { return ensure_staging(f, bytes); }
 
-int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout, double t_end, long long max_steps,
-              int stop_on_error, const hc_init* init, int sync) {
+// The host side of an admission: the slot's device memory (zeroed on the
+// stream), its descriptor and control block in the pinned mirrors and its
+// tensor maps; uploading them is the caller's (upload_slots).
+static int add_host(FusedSet* f, int slot, const hc_solver_desc& d, double t_end, long long max_steps,
+                    int stop_on_error) {
     if (slot < 0 || slot >= f->max_slots || f->slots[slot].used) return fail(HC_ERR_STATE, "slot unavailable");
     HC_CHECK(validate(f, d));
     Slot& S = f->slots[slot];
@@ -579,13 +584,31 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     for (int b = 0; b < nd; ++b, p += planeBytes * 5) I.dbuf[b] = p;
     S.used = true;
     f->h_inst_up[slot] = I;
-    HC_CUDA(cudaMemcpyAsync(f->d_inst + slot, &f->h_inst_up[slot], sizeof(DevInst), cudaMemcpyHostToDevice, f->stream));
     DevCtl& c = f->h_ctl_up[slot];
     std::memset(&c, 0, sizeof(c));
     c.dtmin[0] = c.dtmin[1] = kInfBits;
     c.active = 1;
-    HC_CUDA(cudaMemcpyAsync(f->d_ctl + slot, &c, sizeof(DevCtl), cudaMemcpyHostToDevice, f->stream));
-    int r = encode_maps(f, slot);
+    int const r = encode_maps(f, slot, false);
+    if (r != HC_OK) fused_remove(f, slot);
+    return r;
+}
+
+// Descriptors, control blocks and tensor maps of slots [lo, hi) from the
+// pinned mirrors, one copy each.
+static int upload_slots(FusedSet* f, int lo, int hi) {
+    size_t const n = (size_t)(hi - lo);
+    HC_CUDA(cudaMemcpyAsync(f->d_inst + lo, &f->h_inst_up[lo], sizeof(DevInst) * n, cudaMemcpyHostToDevice, f->stream));
+    HC_CUDA(cudaMemcpyAsync(f->d_ctl + lo, &f->h_ctl_up[lo], sizeof(DevCtl) * n, cudaMemcpyHostToDevice, f->stream));
+    HC_CUDA(cudaMemcpyAsync(f->d_tmaps + (size_t)lo * kMaxBufs, &f->h_tmaps[(size_t)lo * kMaxBufs],
+                            sizeof(CUtensorMap) * kMaxBufs * n, cudaMemcpyHostToDevice, f->stream));
+    return HC_OK;
+}
+
+int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, int layout, double t_end, long long max_steps,
+              int stop_on_error, const hc_init* init, int sync) {
+    HC_CHECK(add_host(f, slot, d, t_end, max_steps, stop_on_error));
+    Slot& S = f->slots[slot];
+    int r = upload_slots(f, slot, slot + 1);
     if (r == HC_OK && has_fixed(S))
         find_aux(f->sch.precision, S.dim)->fixed_ghosts(f->d_inst, slot, f->plan[0].n_state_bufs, f->stream);
     if (r == HC_OK && host) r = set_state(f, slot, host, layout, 1, true);
@@ -596,6 +619,98 @@ int fused_add(FusedSet* f, int slot, const hc_solver_desc& d, const void* host, 
     }
     f->items_dirty = true;
     if (sync) HC_CUDA(cudaStreamSynchronize(f->stream));
+    return HC_OK;
+}
+
+// The device address of a host buffer in page-locked memory (cudaMallocHost,
+// cudaHostRegister), which kernels read and write in place over the host link;
+// nullptr for pageable memory.
+static void* pinned_device_ptr(const void* host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// n admissions from host states in one pass: the host side of each, then the
+// uploads of the slots' descriptors in runs of consecutive slots, then every
+// state set up by its own load launch, which reads a page-locked host buffer
+// in place and otherwise its own range of one staging buffer, all queued back
+// to back (no wait).  Stops at the first instance the host side refuses;
+// *n_done = the instances admitted.
+int fused_add_many(FusedSet* f, int n, const int* slots, const hc_solver_desc* descs, const void* const* hosts,
+                   int layout, const double* t_end, const long long* max_steps, int stop_on_error, int* n_done) {
+    *n_done = 0;
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    int r = HC_OK;
+    int k = 0;
+    for (; k < n; ++k) {
+        r = add_host(f, slots[k], descs[k], t_end[k], max_steps[k], stop_on_error);
+        if (r != HC_OK) break;
+    }
+    int const done = k;
+    *n_done = done;
+    if (!done) return r;
+    std::vector<int> sorted(slots, slots + done);
+    std::sort(sorted.begin(), sorted.end());
+    for (size_t a = 0; a < sorted.size();) {
+        size_t b = a + 1;
+        while (b < sorted.size() && sorted[b] == sorted[b - 1] + 1) ++b;
+        HC_CHECK(upload_slots(f, sorted[a], sorted[b - 1] + 1));
+        a = b;
+    }
+    std::vector<void*> direct(done);
+    std::vector<size_t> off(done + 1, 0);
+    for (int j = 0; j < done; ++j) {
+        direct[j] = pinned_device_ptr(hosts[j]);
+        off[j + 1] = off[j] + (direct[j] ? 0 : round_up(layout_bytes(f->slots[slots[j]].cells, layout), 256));
+    }
+    if (off[done]) HC_CHECK(ensure_staging(f, off[done]));
+    for (int j = 0; j < done; ++j) {
+        Slot& S = f->slots[slots[j]];
+        const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
+        if (has_fixed(S)) A->fixed_ghosts(f->d_inst, slots[j], f->plan[0].n_state_bufs, f->stream);
+        void* src = direct[j];
+        if (!src) {
+            src = static_cast<char*>(f->staging) + off[j];
+            HC_CUDA(cudaMemcpyAsync(src, hosts[j], layout_bytes(S.cells, layout), cudaMemcpyHostToDevice, f->stream));
+        }
+        A->load(f->d_inst, f->d_ctl, slots[j], 0, src, layout, 1, S.cells, f->stream);
+        if (has_extrap(S)) A->extrap_slot(f->d_inst, slots[j], 0, f->stream);
+    }
+    HC_CUDA(cudaGetLastError());
+    f->items_dirty = true;
+    return r;
+}
+
+// n fetches in one pass: every slot's state gathered by its own launch,
+// straight into a page-locked host buffer, otherwise into its own range of one
+// staging buffer (the gathers back to back) and copied out from there (the
+// copies back to back); no wait.
+int fused_get_state_many(FusedSet* f, int n, const int* slots, void* const* hosts, int layout) {
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    std::vector<void*> direct(n);
+    std::vector<size_t> off(n + 1, 0);
+    for (int j = 0; j < n; ++j) {
+        const Slot& S = f->slots[slots[j]];
+        if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+        direct[j] = pinned_device_ptr(hosts[j]);
+        off[j + 1] = off[j] + (direct[j] ? 0 : round_up(layout_bytes(S.cells, layout), 256));
+    }
+    if (off[n]) HC_CHECK(ensure_staging(f, off[n]));
+    for (int j = 0; j < n; ++j) {
+        const Slot& S = f->slots[slots[j]];
+        void* const dst = direct[j] ? direct[j] : static_cast<char*>(f->staging) + off[j];
+        find_aux(f->sch.precision, S.dim)->xfer(f->d_inst, slots[j], state_buf(f, slots[j]), dst, layout, 1, S.cells,
+                                                 f->stream);
+    }
+    HC_CUDA(cudaGetLastError());
+    for (int j = 0; j < n; ++j)
+        if (!direct[j])
+            HC_CUDA(cudaMemcpyAsync(hosts[j], static_cast<char*>(f->staging) + off[j],
+                                    layout_bytes(f->slots[slots[j]].cells, layout), cudaMemcpyDeviceToHost, f->stream));
     return HC_OK;
 }
 
@@ -1120,6 +1235,7 @@ void register_f32_d3c(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_m2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_m3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_m2b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -1138,6 +1254,7 @@ void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>
     register_f32_d3(st, aux);
     register_f32_m2(st, aux);
     register_f32_m3(st, aux);
+    register_f32_m2b(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);
     register_f64_d3(st, aux);

@@ -157,6 +157,10 @@ int init_validate(const hc_init& ic, const hc_solver_desc& d);
 int init_fill(const hc_init& ic, const hc_solver_desc& d, double* dst, cudaStream_t s);
 // sync = 0 leaves the copy queued (the caller synchronises before reading)
 int fused_get_state(FusedSet* f, int slot, void* host, int layout, int sync = 1);
+// many admissions from host states / many fetches, queued in one pass (no wait)
+int fused_add_many(FusedSet* f, int n, const int* slots, const hc_solver_desc* descs, const void* const* hosts,
+                   int layout, const double* t_end, const long long* max_steps, int stop_on_error, int* n_done);
+int fused_get_state_many(FusedSet* f, int n, const int* slots, void* const* hosts, int layout);
 size_t fused_state_bytes(const FusedSet* f, int slot, int layout);
 int fused_reserve_staging(FusedSet* f, size_t bytes);
 // Runs `steps` updates of every live instance (device-side completion tests).

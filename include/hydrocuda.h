@@ -343,11 +343,14 @@ int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* 
                         double t_end, long long max_steps, unsigned long long tag, int* slot);
 /* `count` hc_batch_admit calls in one: instance k from descs[k], cons[k],
  * t_end[k], max_steps[k], tags[k] (t_end, max_steps, tags may be NULL: +inf,
- * no limit, k), all in `layout`.  The uploads and set-up launches of every
- * instance are queued back to back and waited for once, so with pinned host
- * buffers the host's launch work overlaps the device's copies.  Stops at the
- * first refusal or error and returns it; *n_admitted = the instances admitted
- * before it (they stay admitted), slots[k] their slots, -1 for the rest. */
+ * no limit, k), all in `layout`.  Every instance is checked first; the
+ * descriptors of the accepted ones are uploaded together and their set-up
+ * launches queued back to back and waited for once.  A buffer in page-locked
+ * host memory (hc_host_alloc, cudaHostRegister) is read in place by its
+ * set-up kernel over the host link; other buffers go through a staging copy.
+ * Stops at the first refusal or error and returns it; *n_admitted = the
+ * instances admitted before it (they stay admitted), slots[k] their slots, -1
+ * for the rest. */
 int hc_batch_admit_many(hc_batch* b, int count, const hc_solver_desc* descs, const void* const* cons, int layout,
                         const double* t_end, const long long* max_steps, const unsigned long long* tags,
                         int* slots, int* n_admitted);
@@ -378,8 +381,9 @@ int hc_batch_list(hc_batch* b, hc_done* out, int cap, int* n_out);
 /* Copies a slot's interior state to the host. */
 int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout);
 /* `count` hc_batch_fetch calls in one (slot slots[k] into cons[k], all in
- * `layout`), queued back to back and waited for once.  Checks every slot
- * before copying anything. */
+ * `layout`), queued back to back and waited for once; a page-locked buffer is
+ * written in place by its gather kernel.  Checks every slot before copying
+ * anything. */
 int hc_batch_fetch_many(hc_batch* b, int count, const int* slots, void* const* cons, int layout);
 /* Frees a slot and returns its bytes to the budget. */
 int hc_batch_retire(hc_batch* b, int slot);

@@ -370,6 +370,10 @@ def main():
     if rank == 0 and not args.no_e2e:
         out["e2e"] = e2e_run(hc, ctx, work, inputs, cells, st["schedule"][1])
     if rank == 0:
+        # the arithmetic ceilings beside the HBM roofline (the stage kernels
+        # are bound by their instruction streams)
+        out["alu_peaks"] = {"fp32_tflops": hc.measure_fma("f32"), "fp64_tflops": hc.measure_fma("f64"),
+                            "note": "FMA throughput of a kernel of independent FMA chains (hc_measure_fma)"}
         if not args.no_fp64:
             out["fp64"] = fp64_run(hc, ctx, work)
         if not args.no_serving:

@@ -152,6 +152,7 @@ PROTOTYPES = {
     "hc_solver_calc_dt": (_ip, [_vp, _dp]),
     "hc_solver_step": (_ip, [_vp, ctypes.c_double]),
     "hc_solver_update": (_ip, [_vp, _dp]),
+    "hc_measure_fma": (_ip, [_ip, _dp]),
     "hc_solver_stage": (_ip, [_vp, ctypes.c_double]),
     "hc_solver_num_stages": (_ip, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "hc_solver_get_slab": (_ip, [_vp, _ip, _ip, _dp]),
@@ -217,6 +218,14 @@ def load_library(path=None):
 def _check(code):
     if code != HC_OK:
         raise HydroCudaError(code, _lib.hc_last_error().decode())
+
+
+def measure_fma(precision="f32"):
+    """The current device's FMA throughput in TFLOP/s (hc_measure_fma)."""
+    L = load_library()
+    v = ctypes.c_double()
+    _check(L.hc_measure_fma(PRECISIONS[precision], ctypes.byref(v)))
+    return v.value
 
 
 def device_count():

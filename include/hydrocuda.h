@@ -212,6 +212,11 @@ typedef struct hc_batch   hc_batch;
 const char* hc_version(void);
 /* Message of the last failed call on this thread ("" if none). */
 const char* hc_last_error(void);
+/* Measurement aid (no counterpart in the reference): the current device's
+ * fused multiply-add throughput in TFLOP/s (2 flops per FMA), from a kernel of
+ * independent FMA chains; precision HC_F32_FUSED (FP32) or HC_F64_FUSED /
+ * HC_F64_PLAIN (FP64). */
+int hc_measure_fma(int precision, double* tflops);
 /* Number of visible CUDA devices. */
 int hc_device_count(int* count);
 /* One context per device; owns the streams the handles below use.

@@ -179,6 +179,11 @@ struct FusedSet {
     int grid[3] = {0, 0, 0};
     // graph of one (or two, when the state rotates) steps
     cudaGraphExec_t graph = nullptr;
+    // a branch per grid dimension inside the graph: the dimensions' stage
+    // launches are independent, so an underfilled launch of one overlaps the
+    // others (side streams and events used only while capturing)
+    cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
     bool graph_valid = false;
     int extrap_dims = 0;           // dims (bit d-1) whose live instances have a linear / quadratic boundary
     int graph_dims_mask = 0;
@@ -318,6 +323,11 @@ void fused_destroy(FusedSet* f) {
     if (f->h_inst_up) cudaFreeHost(f->h_inst_up);
     if (f->h_ctl_up) cudaFreeHost(f->h_ctl_up);
     if (f->graph) cudaGraphExecDestroy(f->graph);
+    for (int d = 0; d < 3; ++d) {
+        if (f->side[d]) cudaStreamDestroy(f->side[d]);
+        if (f->join[d]) cudaEventDestroy(f->join[d]);
+    }
+    if (f->fork) cudaEventDestroy(f->fork);
     delete f;
 }
 
@@ -809,7 +819,8 @@ static void fill_stage(StageDev& sd, const StagePlan& sp, int stage) {
 
 // Launches the stages of one step with plan p (k_begin / k_set_dt around it
 // are the caller's).
-static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
+static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask, cudaStream_t stream = nullptr) {
+    if (!stream) stream = f->stream;
     for (int s = 0; s < P.n_stages; ++s) {
         for (int d = 0; d < 3; ++d) {
             if (!(dims_mask & (1 << d))) continue;
@@ -827,13 +838,13 @@ static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask) {
             a.work = f->d_work + P.stage[s].index * 3 + d;
             a.force_timeout = f->force_timeout;
             fill_stage(a.st, P.stage[s], P.stage[s].index);
-            f->launcher[d]->launch(a, f->sch.slope_limiter, f->sch.flux_limiter, f->grid[d], f->stream);
+            f->launcher[d]->launch(a, f->sch.slope_limiter, f->sch.flux_limiter, f->grid[d], stream);
         }
         // linear / quadratic ghosts of this stage's output, before the next stage reads them
         for (int d = 0; d < 3; ++d)
             if ((dims_mask & f->extrap_dims) & (1 << d))
                 find_aux(f->sch.precision, d + 1)->extrap_stage(f->d_inst, f->d_ctl, f->max_slots, P.stage[s].out_buf,
-                                                                f->rot_buf, f->stream);
+                                                                f->rot_buf, stream);
     }
     HC_CUDA(cudaGetLastError());
     return HC_OK;
@@ -845,11 +856,36 @@ static int launch_step(FusedSet* f, int dims_mask) {
     return launch_stages(f, f->plan[0], dims_mask);
 }
 
+// One step into the capture: k_begin, then each dimension's stages on a
+// branch of its own (forked from and joined back to the batch's stream) when
+// more than one dimension is live.
+static int capture_step(FusedSet* f, int mask) {
+    if ((mask & (mask - 1)) == 0) return launch_step(f, mask);
+    unsigned const g = (unsigned)((f->max_slots + 127) / 128);
+    fz::k_begin<<<g, 128, 0, f->stream>>>(f->d_ctl, f->d_inst, f->max_slots, 1, f->rotates, f->betas, f->d_work);
+    HC_CUDA(cudaEventRecord(f->fork, f->stream));
+    for (int d = 0; d < 3; ++d) {
+        if (!(mask & (1 << d))) continue;
+        HC_CUDA(cudaStreamWaitEvent(f->side[d], f->fork, 0));
+        HC_CHECK(launch_stages(f, f->plan[0], 1 << d, f->side[d]));
+        HC_CUDA(cudaEventRecord(f->join[d], f->side[d]));
+        HC_CUDA(cudaStreamWaitEvent(f->stream, f->join[d], 0));
+    }
+    return HC_OK;
+}
+
 static int capture_graph(FusedSet* f) {
     if (f->graph) { cudaGraphExecDestroy(f->graph); f->graph = nullptr; }
+    if (!f->fork) {
+        HC_CUDA(cudaEventCreateWithFlags(&f->fork, cudaEventDisableTiming));
+        for (int d = 0; d < 3; ++d) {
+            HC_CUDA(cudaStreamCreateWithFlags(&f->side[d], cudaStreamNonBlocking));
+            HC_CUDA(cudaEventCreateWithFlags(&f->join[d], cudaEventDisableTiming));
+        }
+    }
     cudaGraph_t g;
     HC_CUDA(cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal));
-    int r = launch_step(f, f->graph_dims_mask);
+    int r = capture_step(f, f->graph_dims_mask);
     cudaError_t e = cudaStreamEndCapture(f->stream, &g);
     if (r != HC_OK) { if (e == cudaSuccess) cudaGraphDestroy(g); return r; }
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");

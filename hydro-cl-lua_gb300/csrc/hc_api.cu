@@ -458,6 +458,14 @@ int hc_solver_stage(hc_solver* s, double dt) {
     return fused_sync(s->fused);
 }
 
+int hc_solver_autotune(hc_solver* s, const char* cache_path) {
+    if (!s) return fail(HC_ERR_INVALID, "NULL solver");
+    if (s->plain) return HC_OK;   // one kernel set: nothing to choose
+    if (s->next_stage) return fail(HC_ERR_STATE, "an update run stage by stage is in progress");
+    HC_CHECK(use_device(s->ctx));
+    return fused_autotune_keep(s->fused, 0, cache_path);
+}
+
 int hc_solver_num_stages(hc_solver* s, int* n) {
     if (!s || !n) return fail(HC_ERR_INVALID, "NULL argument");
     if (s->plain) return fail(HC_ERR_INVALID, "the plain form steps whole updates (hc_solver_step)");

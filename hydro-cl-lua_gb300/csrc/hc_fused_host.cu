@@ -1244,6 +1244,35 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
 
 int fused_variant(const FusedSet* f, int dim) { return f->launcher[dim - 1] ? f->launcher[dim - 1]->variant : -1; }
 
+// fused_autotune without advancing one slot's solve (a single solver): its
+// state buffer, ghosts included, and its control block are copied aside on the
+// device before the timed steps and put back after them.
+int fused_autotune_keep(FusedSet* f, int slot, const char* cache_path) {
+    Slot& S = f->slots[slot];
+    if (!S.used) return fail(HC_ERR_STATE, "slot not in use");
+    int const b = state_buf(f, slot);
+    size_t const bytes = (size_t)S.inst.plane * 5 * f->esize;
+    void* save = nullptr;
+    DevCtl* ctl = nullptr;
+    HC_CUDA(cudaMalloc(&save, bytes));
+    cudaError_t e = cudaMalloc(&ctl, sizeof(DevCtl));
+    if (e != cudaSuccess) { cudaFree(save); return cuda_fail(e, "cudaMalloc"); }
+    int r = HC_OK;
+    e = cudaMemcpyAsync(save, S.inst.buf[b], bytes, cudaMemcpyDeviceToDevice, f->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, f->d_ctl + slot, sizeof(DevCtl), cudaMemcpyDeviceToDevice, f->stream);
+    if (e != cudaSuccess) r = cuda_fail(e, "cudaMemcpyAsync");
+    if (r == HC_OK) r = fused_autotune(f, cache_path);
+    // put the solve back even if tuning failed part way
+    e = cudaMemcpyAsync(S.inst.buf[b], save, bytes, cudaMemcpyDeviceToDevice, f->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(f->d_ctl + slot, ctl, sizeof(DevCtl), cudaMemcpyDeviceToDevice, f->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(f->stream);
+    cudaFree(save);
+    cudaFree(ctl);
+    if (e != cudaSuccess && r == HC_OK) r = cuda_fail(e, "restoring the solve after tuning");
+    f->items_dirty = true;
+    return r;
+}
+
 int fused_set_schedule(FusedSet* f, int dim, int variant) {
     if (!find_launcher(f->sch, dim, variant)) return fail(HC_ERR_INVALID, "no such schedule for this scheme and dimension");
     HC_CUDA(cudaStreamSynchronize(f->stream));

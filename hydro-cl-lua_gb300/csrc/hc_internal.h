@@ -186,6 +186,8 @@ int fused_variant(const FusedSet* f, int dim);
 int fused_conservation(FusedSet* f, int slot, double sums[5]);
 int fused_stats(FusedSet* f, hc_batch_stats* st);
 int fused_autotune(FusedSet* f, const char* cache_path);
+// fused_autotune that leaves slot `slot`'s solve as it was
+int fused_autotune_keep(FusedSet* f, int slot, const char* cache_path);
 int fused_set_schedule(FusedSet* f, int dim, int variant);
 int fused_sync(FusedSet* f);
 

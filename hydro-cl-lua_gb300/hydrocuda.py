@@ -153,6 +153,7 @@ PROTOTYPES = {
     "hc_solver_step": (_ip, [_vp, ctypes.c_double]),
     "hc_solver_update": (_ip, [_vp, _dp]),
     "hc_measure_fma": (_ip, [_ip, _dp]),
+    "hc_solver_autotune": (_ip, [_vp, ctypes.c_char_p]),
     "hc_solver_stage": (_ip, [_vp, ctypes.c_double]),
     "hc_solver_num_stages": (_ip, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "hc_solver_get_slab": (_ip, [_vp, _ip, _ip, _dp]),
@@ -525,6 +526,11 @@ class Solver:
         dt = ctypes.c_double()
         _check(self.L.hc_solver_update(self.h, ctypes.byref(dt)))
         return dt.value
+
+    def autotune(self, cache_path=None):
+        """Picks the fused forms' fastest stage-kernel schedule for this grid
+        (hc_solver_autotune); the solve is left as it was."""
+        _check(self.L.hc_solver_autotune(self.h, cache_path.encode() if cache_path else None))
 
     # one grid cut into slabs (see hc_solver_stage in the header)
     @property

@@ -92,6 +92,9 @@ function CudaFVSolver:init(args)
 	self.hcSolver = ffi.gc(p[0], hc.lib.hc_solver_destroy)
 	self.hcPlain = desc.precision == 0
 	self.hcNeedsUpload = true
+	-- the fused forms pick their fastest stage-kernel schedule for this grid
+	-- once the state is set (cudaAutotune = false keeps the default one)
+	self.hcAutotune = not self.hcPlain and args.cudaAutotune ~= false
 end
 
 -- The update's OpenCL kernels (calcLR, calcFlux, calcDerivFromFlux) are
@@ -182,6 +185,11 @@ function CudaFVSolver:resetState()
 	CudaFVSolver.super.resetState(self)
 	self:syncFromCL()
 	hc.check(hc.lib.hc_solver_set_time(self.hcSolver, 0))
+	if self.hcAutotune then
+		-- leaves the state and time as they are
+		hc.check(hc.lib.hc_solver_autotune(self.hcSolver, nil))
+		self.hcAutotune = false
+	end
 end
 
 function CudaFVSolver:boundary()

@@ -49,6 +49,7 @@ int hc_solver_constrain_u(hc_solver* s);
 int hc_solver_calc_dt(hc_solver* s, double* dt);
 int hc_solver_step(hc_solver* s, double dt);
 int hc_solver_update(hc_solver* s, double* dt_out);
+int hc_solver_autotune(hc_solver* s, const char* cache_path);
 int hc_solver_run_until(hc_solver* s, double t_end, long long max_steps, long long* steps_done);
 int hc_solver_get_time(hc_solver* s, double* t);
 int hc_solver_set_time(hc_solver* s, double t);

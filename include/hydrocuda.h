@@ -259,6 +259,11 @@ int hc_solver_calc_dt(hc_solver* s, double* dt);
 int hc_solver_step(hc_solver* s, double dt);
 /* SolverBase:update() (solverbase.lua:3026): calcDT, step, t += dt, boundary. */
 int hc_solver_update(hc_solver* s, double* dt_out);
+/* The fused forms' stage-kernel schedule for this solver's grid, chosen as
+ * hc_batch_autotune chooses it (every schedule gives the same bits), without
+ * advancing the solve: its state and time are as before the call.  No-op on
+ * the plain form.  No counterpart in the reference. */
+int hc_solver_autotune(hc_solver* s, const char* cache_path);
 /* ---- one grid cut into slabs across devices or ranks --------------------------
  *
  * The reference's multi-device solver (hydro/solver/choppedup.lua) cuts a

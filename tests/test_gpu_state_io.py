@@ -75,3 +75,31 @@ def test_snapshot_restart_from_fits(hc, ctx, tmp_path):
         a.update()
         b.update()
         np.testing.assert_array_equal(b.getState(), a.getState(), err_msg=prec)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_solver_autotune_keeps_the_solve(hc, ctx, dim):
+    """hc_solver_autotune times the schedules on the solver's own grid and puts
+    its state and time back: the solve goes on exactly as an untuned one."""
+    import cases
+    if dim == 2:
+        a = cases.c4_quadrant(96)
+        u = hc.quadrant_state(a, hc.random_quadrants(hc.SplitMix64(12)))
+    else:
+        a = cases.c3_blast(24)
+        u = hc.blast_state(a)
+    tuned = hc.Solver(ctx, precision="f32", **a)
+    plain = hc.Solver(ctx, precision="f32", **a)
+    for s in (tuned, plain):
+        s.resetState(u)
+        s.update()
+    before = tuned.getState(withGhosts=True)
+    t0 = tuned.t
+    tuned.autotune()
+    np.testing.assert_array_equal(tuned.getState(withGhosts=True), before)
+    assert tuned.t == t0
+    for _ in range(3):
+        tuned.update()
+        plain.update()
+    np.testing.assert_array_equal(tuned.getState(), plain.getState())
+    assert tuned.t == plain.t

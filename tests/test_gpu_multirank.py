@@ -73,6 +73,9 @@ CASES = {
     "kh-periodic-rk3tvd": cases.c2_kh(32, integrator="Runge-Kutta 3, TVD", gridSize=[32, 30]),
     "kh-freeflow-rk3tvd": cases.c2_kh(32, integrator="Runge-Kutta 3, TVD", gridSize=[32, 30], boundary="freeflow"),
     "sod-freeflow-rk4": cases.c1_sod(integrator="Runge-Kutta 4", gridSize=[256]),
+    # forward Euler alternates the state between two buffers (the slab calls
+    # follow the rotation)
+    "kh-periodic-fe": cases.c2_kh(32, integrator="forward Euler", gridSize=[32, 30]),
     "blast-freeflow-rk2": cases.c3_blast(12, gridSize=[12, 10, 14]),
 }
 

@@ -222,7 +222,9 @@ def run_reference(args):
     work = workload()
     oracle.build()
     solvers = []
-    budget_cells = 6_000_000   # about one to a few seconds of CPU work per step
+    # a bounded sample: at most 6 M cells, fewer when --steps is large, so the
+    # whole run stays near two minutes at the oracle's ~3e7 cell-updates/s
+    budget_cells = int(min(6_000_000, max(250_000, 3e7 * 120 / (args.steps + args.warmup))))
     cells = 0
     for a, q in work:
         s = oracle.OracleSolver(a)

@@ -69,3 +69,40 @@ def test_name_tables_match_the_python_binding():
     assert table("fluxIndex") == {k: i for i, k in enumerate(hydrocuda.FLUXES)}
     assert table("reconIndex") == {k: v for k, v in hydrocuda.RECONS.items() if isinstance(k, str)}
     assert table("renderMode") == hydrocuda.RENDER_MODES
+
+
+def _lua_sources():
+    base = os.path.join(ROOT, "hydro-cl-lua_gb300", "lua")
+    out = []
+    for d, _, files in os.walk(base):
+        out += [os.path.join(d, f) for f in files if f.endswith(".lua")]
+    return out
+
+
+def test_every_library_call_is_declared():
+    """Each hc_* entry point the Lua files call through the ffi library is
+    declared by the binding's cdef (LuaJIT raises on an undeclared symbol only
+    when the call runs) and exported by the header."""
+    declared = set(_functions(_cdef()))
+    exported = set(_functions(_header()))
+    used = set()
+    for path in _lua_sources():
+        used |= set(re.findall(r"\blib\.(hc_\w+)", open(path).read()))
+    assert len(used) >= 15
+    assert used <= declared, sorted(used - declared)
+    assert used <= exported, sorted(used - exported)
+
+
+def test_every_ffi_struct_used_is_declared():
+    """The structs the Lua files create with ffi.new are declared by a cdef."""
+    cdefs = ""
+    for path in _lua_sources():
+        for m in re.finditer(r"ffi\.cdef\[\[(.*?)\]\]", open(path).read(), flags=re.S):
+            cdefs += m.group(1)
+    declared = set(re.findall(r"typedef struct (\w+)", cdefs)) | {"int", "double", "char", "float"}
+    seen = 0
+    for path in _lua_sources():
+        for name in re.findall(r"ffi\.new\s*\(?\s*'(\w+)", open(path).read()):
+            assert name in declared, (path, name)
+            seen += 1
+    assert seen >= 10

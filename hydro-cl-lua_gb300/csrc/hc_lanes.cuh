@@ -771,15 +771,6 @@ __device__ __forceinline__ void constrain(V* u, const Eos& s, float invg1) {
     u[4] = sel(fix, fma(P, splat<V>(invg1), mul(rho, mul(splat<V>(.5f), vsq))), u[4]);
 }
 
-// For callers where every lane of the warp takes part (the marching
-// kernels' epilogues): constrain() with the clamp taken only when a lane
-// needs it (a warp-uniform test), then, when `last`, the cell's CFL dt.  An
-// unclamped lane's state is unchanged, so its 1/rho, |m|^2 and P are the values
-// dtCell would compute from it, and are reused; a warp with a clamped lane
-// evaluates dtCell.  The same bits as constrain() followed by dtCell().
-template <int DIM>
-__device__ __forceinline__ float constrainDtWarp(float* u, const Eos& s, float invg1, bool last, const float* gdx);
-
 // calcDTCell (calcDT.cl:38-73): min over the active sides of
 // dx / max(|vn - Cs|, |vn + Cs|, 1e-9), with Cs = 0 where P <= PMin and
 // infinite where rho < rhoMin.
@@ -800,34 +791,6 @@ __device__ __forceinline__ V dtCell(const V* u, const Eos& s, const float* gdx) 
         V a = vmax(absv(sub(vn, Cs)), absv(add(vn, Cs)));
         a = vmax(splat<V>(1e-9f), a);
         dt = vmin(dt, mul(splat<V>(gdx[side]), rcp(a)));
-    }
-    return dt;
-}
-
-template <int DIM>
-__device__ __forceinline__ float constrainDtWarp(float* u, const Eos& s, float invg1, bool last, const float* gdx) {
-    float const inf = __int_as_float(0x7f800000);
-    // below rhoMin, or NaN (max() would hide it in 1/rho)
-    bool const thin = !(u[0] >= s.rhoMin);
-    float const rho = vmax(u[0], s.rhoMin);
-    float const inv = rcp(rho);
-    float const m2 = fma(u[3], u[3], fma(u[2], u[2], mul(u[1], u[1])));
-    float const P0 = mul(s.g1, fma(mul(-.5f, m2), inv, u[4]));
-    bool const low = lt(P0, s.PMin);
-    if (__any_sync(0xffffffffu, thin || low)) {
-        constrain<float>(u, s, invg1);
-        return last ? dtCell<float, DIM>(u, s, gdx) : inf;
-    }
-    if (!last) return inf;
-    float Cs = sqr(mul(mul(s.gamma, P0), inv));
-    Cs = sel(le(P0, s.PMin), 0.f, Cs);
-    float dt = inf;
-#pragma unroll
-    for (int side = 0; side < DIM; ++side) {
-        float const vn = mul(u[1 + side], inv);
-        float a = vmax(absv(sub(vn, Cs)), absv(add(vn, Cs)));
-        a = vmax(1e-9f, a);
-        dt = vmin(dt, mul(gdx[side], rcp(a)));
     }
     return dt;
 }

@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
 #pragma unroll
                         for (int f = 0; f < 5; ++f) u[f] = lanes::fma(deriv[f], cbcur, u[f]);
                     }
-                    float const dtc = lanes::constrainDtWarp<2>(u, le, K.invg1, st.last, K.gdx);
+                    lanes::constrain<float>(u, le, K.invg1);
                     if (inCols) {
 #pragma unroll
                         for (int f = 0; f < 5; ++f) out[f * geo.plane + idx] = u[f];
@@ -409,7 +409,10 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                     bad |= inCols && !fast::M<float>::finite_(u[0] + u[4]);
                     if (edgeX || yc < 2 || yc >= ny - 2)
                         if (inCols) marchGhosts(out, geo.plane, geo.px, nx, ny, geo.bc, x, yc, idx, u);
-                    if (st.last && inCols) dtmin = fast::tmin(dtmin, dtc);
+                    if (st.last) {
+                        float const dtc = lanes::dtCell<float, 2>(u, le, K.gdx);
+                        if (inCols) dtmin = fast::tmin(dtmin, dtc);
+                    }
                 }
             }
 #pragma unroll

@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
 #pragma unroll
                         for (int f = 0; f < 5; ++f) u[f] = lanes::fma(deriv[f], cbcur, u[f]);
                     }
-                    float const dtc = lanes::constrainDtWarp<3>(u, le, K.invg1, st.last, K.gdx);
+                    lanes::constrain<float>(u, le, K.invg1);
                     if (inCols) {
 #pragma unroll
                         for (int f = 0; f < 5; ++f) out[f * geo.plane + idx] = u[f];
@@ -425,7 +425,10 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                         if (edgeXY) marchGhosts(out, geo.plane, geo.px, nx, ny, geo.bc, x, yw, idx, u);
                         if (zc < 2 || zc >= nz - 2) marchGhostsZ(out, geo.plane, ps, nz, geo.bc, zc, idx, u);
                     }
-                    if (st.last && inCols) dtmin = fast::tmin(dtmin, dtc);
+                    if (st.last) {
+                        float const dtc = lanes::dtCell<float, 3>(u, le, K.gdx);
+                        if (inCols) dtmin = fast::tmin(dtmin, dtc);
+                    }
                 }
             }
             if (tileRow) {

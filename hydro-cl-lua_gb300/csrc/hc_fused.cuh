@@ -135,6 +135,7 @@ struct StageArgs {
     int recon;                  // HC_RECON_*
     int* work;                  // marching kernels: this launch's work counter (zeroed when the step begins)
     int force_timeout;          // test knob, 0 in normal use: the first wait for each copy counts as run out
+    const int* seg;             // marching kernels: rows (2D) / planes (3D) per segment of the item list
 };
 
 // Work counters of the marching kernels: one per (stage, dimension), zeroed by

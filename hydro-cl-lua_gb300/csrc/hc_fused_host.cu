@@ -171,12 +171,14 @@ struct FusedSet {
     // work lists per dimension
     int4* d_items[3] = {nullptr, nullptr, nullptr};
     size_t items_cap[3] = {0, 0, 0};
-    int* d_nitems = nullptr;       // [3]
-    int h_nitems[3] = {0, 0, 0};
+    int* d_nitems = nullptr;       // [6]: items per dimension, then the marching segment length per dimension
+    int h_nitems[6] = {0, 0, 0, 0, 0, 0};
     bool items_dirty = true;
     // chosen tile-shape variant per dimension
     const StageLauncher* launcher[3] = {nullptr, nullptr, nullptr};
     int grid[3] = {0, 0, 0};
+    int seg[3] = {0, 0, 0};        // marching launchers: rows (2D) / planes (3D) per segment of the item list
+    int seg_fixed = 0;             // HC_MARCH_SEGMENT at creation: segments of min(this, the schedule's); 0 balanced
     // graph of one (or two, when the state rotates) steps
     cudaGraphExec_t graph = nullptr;
     // a branch per grid dimension inside the graph: the dimensions' stage
@@ -246,6 +248,9 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
         // test knob for the bounded-wait path; off unless the variable is "1"
         const char* ft = std::getenv("HC_TEST_FORCE_TIMEOUT");
         f->force_timeout = ft && ft[0] == '1' && ft[1] == 0;
+        // tuning knob: a fixed marching segment length instead of the balanced one
+        const char* sg = std::getenv("HC_MARCH_SEGMENT");
+        f->seg_fixed = sg ? std::max(0, std::atoi(sg)) : 0;
     }
     f->esize = sch.precision == HC_F32_FUSED ? 4 : 8;
     f->max_slots = max_slots;
@@ -274,7 +279,7 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
     A((void**)&f->d_tmaps, sizeof(CUtensorMap) * kMaxBufs * max_slots);
     A((void**)&f->d_err, sizeof(int));
     A((void**)&f->d_work, sizeof(int) * kWorkCounters);
-    A((void**)&f->d_nitems, sizeof(int) * 3);
+    A((void**)&f->d_nitems, sizeof(int) * 6);
     A((void**)&f->d_partial, sizeof(double) * 5 * 1024);
     auto H = [&](void** p, size_t b) {
         if (r != HC_OK) return;
@@ -292,7 +297,7 @@ int fused_create(const FusedScheme& sch, int max_slots, cudaStream_t stream, Fus
         cudaMemsetAsync(f->d_tmaps, 0, sizeof(CUtensorMap) * kMaxBufs * max_slots, stream);
         cudaMemsetAsync(f->d_err, 0, sizeof(int), stream);
         cudaMemsetAsync(f->d_work, 0, sizeof(int) * kWorkCounters, stream);
-        cudaMemsetAsync(f->d_nitems, 0, sizeof(int) * 3, stream);
+        cudaMemsetAsync(f->d_nitems, 0, sizeof(int) * 6, stream);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) r = cuda_fail(e, "cudaMemsetAsync");
     }
@@ -738,6 +743,43 @@ int fused_remove(FusedSet* f, int slot) {
     return HC_OK;
 }
 
+// Segment length of a marching launcher's items over the active instances of
+// dimension d + 1 (h_ctl current).  The schedule's own length, unless its
+// items would fill fewer than two rounds of the launch's resident warps (2D:
+// a warp per item) or CTAs (3D): then the length among 4 .. the schedule's
+// that minimises rounds x (length + 4), the 4 rows or planes beside each
+// segment that its box also loads, so one small grid still spreads over
+// every SM.  The bits do not depend on it.
+static int march_segment(const FusedSet* f, int d) {
+    const StageLauncher* L = f->launcher[d];
+    int const full = L->seg;
+    if (f->seg_fixed > 0) return std::min(f->seg_fixed, full);
+    long long const units = (long long)f->grid[d] * (d == 1 ? L->nthreads / 32 : 1);
+    auto count = [&](int h) {
+        long long n = 0;
+        for (int s = 0; s < f->max_slots; ++s) {
+            const Slot& S = f->slots[s];
+            if (!S.used || !f->h_ctl[s].active || S.dim != d + 1) continue;
+            long long const strips = (S.inst.n[0] + L->tx - 1) / L->tx;
+            long long const tiles = d == 2 ? (S.inst.n[1] + L->ty - 1) / L->ty : 1;
+            n += strips * tiles * ((S.inst.n[d] + h - 1) / h);
+        }
+        return n;
+    };
+    long long const nfull = count(full);
+    if (nfull == 0 || nfull >= 2 * units) return full;
+    int best = full;
+    long long bestCost = (long long)((nfull + units - 1) / units) * (full + 4);
+    for (int h = full - 1; h >= 4; --h) {
+        long long const cost = (long long)((count(h) + units - 1) / units) * (h + 4);
+        if (cost < bestCost) {
+            best = h;
+            bestCost = cost;
+        }
+    }
+    return best;
+}
+
 // Rebuilds the per-dimension (slot, tile) work lists.  Items are ordered by
 // slot, then z, y, x tile, so consecutive CTAs work on neighbouring tiles and
 // share halo rows in L2.
@@ -745,6 +787,12 @@ static int rebuild_items(FusedSet* f) {
     if (!f->items_dirty) return HC_OK;
     HC_CUDA(cudaStreamSynchronize(f->stream));
     HC_CUDA(cudaMemcpy(f->h_ctl, f->d_ctl, sizeof(DevCtl) * f->max_slots, cudaMemcpyDeviceToHost));
+    // read by the marching kernels from device memory, as the item counts
+    // are, so a captured step graph stays valid when they change
+    for (int d = 0; d < 3; ++d) {
+        const StageLauncher* L = f->launcher[d];
+        f->seg[d] = L && L->march ? march_segment(f, d) : 0;
+    }
     std::vector<int4> items[3];
     int extrap = 0;
     for (int s = 0; s < f->max_slots; ++s) {
@@ -753,9 +801,12 @@ static int rebuild_items(FusedSet* f) {
         for (int k = 0; k < 2 * S.dim; ++k)
             if (S.inst.bc[k] == HC_BOUNDARY_LINEAR || S.inst.bc[k] == HC_BOUNDARY_QUADRATIC) extrap |= 1 << (S.dim - 1);
         const StageLauncher* L = f->launcher[S.dim - 1];
+        // a marching launcher's segments run along y (2D) or z (3D)
+        int const ty = L->march && S.dim == 2 ? f->seg[1] : L->ty;
+        int const tz = L->march && S.dim == 3 ? f->seg[2] : L->tz;
         int const ntx = (S.inst.n[0] + L->tx - 1) / L->tx;
-        int const nty = S.dim > 1 ? (S.inst.n[1] + L->ty - 1) / L->ty : 1;
-        int const ntz = S.dim > 2 ? (S.inst.n[2] + L->tz - 1) / L->tz : 1;
+        int const nty = S.dim > 1 ? (S.inst.n[1] + ty - 1) / ty : 1;
+        int const ntz = S.dim > 2 ? (S.inst.n[2] + tz - 1) / tz : 1;
         for (int z = 0; z < ntz; ++z)
             for (int y = 0; y < nty; ++y)
                 for (int x = 0; x < ntx; ++x) items[S.dim - 1].push_back(make_int4(s, x, y, z));
@@ -767,10 +818,11 @@ static int rebuild_items(FusedSet* f) {
     for (int d = 0; d < 3; ++d) {
         const StageLauncher* L = f->launcher[d];
         if (!L || !L->march) continue;
+        int const h = f->seg[d];
         auto rowsOf = [&](const int4& it) {
             const DevInst& I = f->slots[it.x].inst;
-            int const rows = std::min(L->ty, I.n[1] - it.z * L->ty);
-            return d == 2 ? rows * std::min(L->tz, I.n[2] - it.w * L->tz) : rows;
+            if (d == 1) return std::min(h, I.n[1] - it.z * h);
+            return std::min(L->ty, I.n[1] - it.z * L->ty) * std::min(h, I.n[2] - it.w * h);
         };
         std::stable_sort(items[d].begin(), items[d].end(),
                          [&](const int4& a, const int4& b) { return rowsOf(a) > rowsOf(b); });
@@ -790,7 +842,8 @@ static int rebuild_items(FusedSet* f) {
         if (n) HC_CUDA(cudaMemcpyAsync(f->d_items[d], items[d].data(), n * sizeof(int4), cudaMemcpyHostToDevice, f->stream));
         f->h_nitems[d] = (int)n;
     }
-    HC_CUDA(cudaMemcpyAsync(f->d_nitems, f->h_nitems, sizeof(int) * 3, cudaMemcpyHostToDevice, f->stream));
+    for (int d = 0; d < 3; ++d) f->h_nitems[3 + d] = f->seg[d];
+    HC_CUDA(cudaMemcpyAsync(f->d_nitems, f->h_nitems, sizeof(int) * 6, cudaMemcpyHostToDevice, f->stream));
     HC_CUDA(cudaStreamSynchronize(f->stream));
     if (mask != f->graph_dims_mask || extrap != f->extrap_dims) f->graph_valid = false;
     f->graph_dims_mask = mask;
@@ -830,6 +883,7 @@ static int launch_stages(FusedSet* f, const IntegratorPlan& P, int dims_mask, cu
             a.tmaps = f->d_tmaps;
             a.items = f->d_items[d];
             a.nitems = f->d_nitems + d;
+            a.seg = f->d_nitems + 3 + d;
             a.err = f->d_err;
             a.rot_buf = f->rot_buf;
             a.flux = f->sch.flux;
@@ -1222,7 +1276,8 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
             HC_CUDA(cudaStreamSynchronize(f->stream));
             const StageLauncher* Lc = f->launcher[dim - 1];
             log << "# " << key << " variant " << v << " tile " << Lc->tx << "x" << Lc->ty << "x" << Lc->tz << " threads "
-                << Lc->nthreads << " seg " << Lc->seg << " unroll " << Lc->unroll << " ctas/SM " << Lc->min_ctas
+                << Lc->nthreads << " seg " << Lc->seg << " (items: " << f->seg[dim - 1] << ") unroll " << Lc->unroll
+                << " ctas/SM " << Lc->min_ctas
                 << " lanes " << Lc->lanes << " slope " << Lc->slope << " ms/step " << ms / reps << "\n";
             if (ms < bestMs) { bestMs = ms; best = v; }
         }

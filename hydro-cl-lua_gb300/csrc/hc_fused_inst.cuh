@@ -57,8 +57,8 @@ void add_stage(std::vector<StageLauncher>& v) {
     v.push_back(sl);
 }
 
-// A 2D marching schedule (hc_march.cuh): NW warps per CTA, segments of H
-// rows, chunks of C rows in NB buffers, the slope limiter SLOPE compiled in
+// A 2D marching schedule (hc_march.cuh): NW warps per CTA, segments of up
+// to H rows, chunks of C rows in NB buffers, the slope limiter SLOPE compiled in
 // (-1: read at run time), OCC CTAs per SM.
 template <int VAR, int NW, int H, int C, int NB, int SLOPE, int OCC>
 void add_march2(std::vector<StageLauncher>& v) {
@@ -109,7 +109,7 @@ void add_march2(std::vector<StageLauncher>& v) {
 }
 
 // A 3D marching schedule (hc_march3.cuh): tiles of 30 columns by NWY - 1
-// rows (NWY warps per CTA) marching up segments of D planes, NB plane buffers,
+// rows (NWY warps per CTA) marching up segments of up to D planes, NB plane buffers,
 // the slope limiter SLOPE compiled in (-1: read at run time), OCC CTAs per SM.
 template <int VAR, int NWY, int D, int NB, int SLOPE, int OCC>
 void add_march3(std::vector<StageLauncher>& v) {

@@ -1,7 +1,9 @@
 // hc_march.cuh -- the 2D marching stage kernel (FP32 fast form, "plm cons").
 //
 // One warp advances one strip of a grid: 30 interior columns (lanes 1..30;
-// lanes 0 and 31 carry the cells beside the strip) over a segment of H rows.
+// lanes 0 and 31 carry the cells beside the strip) over a segment of seg
+// rows (H, the schedule's segment, unless the host shortens the segments of a
+// launch whose items would leave warps idle).
 // The warp marches up the segment one row per step.  Its lane's column of
 // cells passes through registers: the cell below, the cell and the cell above
 // (the last loaded from shared memory), the cell below's y-side R state and
@@ -129,8 +131,9 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
         int const inBuf = slotBuf(st.in_buf, rot, a.rot_buf);
         Geo const geo = geoOf(I);
         int const nx = geo.n[0], ny = geo.n[1];
-        int const x0 = it.y * kStripW, y0 = it.z * H;
-        int const rows = ny - y0 < H ? ny - y0 : H;
+        int const seg = *a.seg;   // read per item: nothing holds it across the march
+        int const x0 = it.y * kStripW, y0 = it.z * seg;
+        int const rows = ny - y0 < seg ? ny - y0 : seg;
         int const nrows = rows + 4;                  // box rows y0-2 .. y0+rows+1
         int const nchunks = (nrows + C - 1) / C;
         // padded column of the strip's first box column (cell x0-2), rounded

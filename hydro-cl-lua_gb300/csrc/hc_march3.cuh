@@ -1,7 +1,8 @@
 // hc_march3.cuh -- the 3D marching stage kernel (FP32 fast form, "plm cons").
 //
-// One CTA advances one x-y tile of a 3D grid up a segment of D planes along
-// z.  The tile is 30 columns wide (lanes 1..30 of every warp; lanes 0 and 31
+// One CTA advances one x-y tile of a 3D grid up a segment of seg planes
+// along z (D, the schedule's segment, unless the host shortens the segments
+// of a launch whose items would leave CTAs idle).  The tile is 30 columns wide (lanes 1..30 of every warp; lanes 0 and 31
 // carry the columns beside it) and NWY - 1 rows high: warp w holds row
 // y0 - 1 + w, so warp 0 carries the row below the tile.  The planes arrive
 // one at a time by TMA (cp.async.bulk.tensor, box 40 x (NWY+3) x 1 x 5
@@ -115,8 +116,9 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
         int const inBuf = slotBuf(st.in_buf, rot, a.rot_buf);
         Geo const geo = geoOf(I);
         int const nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
-        int const x0 = it.y * kStripW, y0 = it.z * TR, z0 = it.w * D;
-        int const planes = nz - z0 < D ? nz - z0 : D;
+        int const seg = *a.seg;   // read per item: nothing holds it across the march
+        int const x0 = it.y * kStripW, y0 = it.z * TR, z0 = it.w * seg;
+        int const planes = nz - z0 < seg ? nz - z0 : seg;
         int const nplanes = planes + 4;              // box planes z0-2 .. z0+planes+1
         int const pa = x0 & ~3;                      // padded column of cell x0-2, rounded down to 16 bytes
         const CUtensorMap* const map = a.tmaps + (size_t)it.x * kMaxBufs + inBuf;

@@ -407,7 +407,11 @@ int hc_batch_conservation(hc_batch* b, int slot, double sums[5]);
 int hc_batch_autotune(hc_batch* b, const char* cache_path);
 /* Pins the schedule (tile shape, segment length, threads, lanes: the
  * `variant` numbers of the autotuner's log) of the stage kernel for grids of
- * dimension `dim`.  HC_ERR_INVALID if this scheme has no such schedule. */
+ * dimension `dim`.  HC_ERR_INVALID if this scheme has no such schedule.
+ * A marching schedule's segments are shortened when its items would fill
+ * fewer than two rounds of the launch's resident warps (2D) or CTAs (3D), as
+ * for one small grid; HC_MARCH_SEGMENT=<rows> in the environment when the
+ * batch is created fixes them at min(rows, the schedule's) instead. */
 int hc_batch_set_schedule(hc_batch* b, int dim, int variant);
 
 /* ---- headless visualisation ----------------------------------------------------

@@ -16,6 +16,13 @@ MARCH = 16      # the marching schedule's number
 TILE = 10       # a tile schedule with every compiled-in limiter
 
 
+@pytest.fixture(autouse=True)
+def full_segments(monkeypatch):
+    """The schedule's own segment length: these small batches would otherwise
+    be cut into short balanced segments (tested on their own below)."""
+    monkeypatch.setenv("HC_MARCH_SEGMENT", "100000")
+
+
 def _run(hc, ctx, probs, scheme, schedule, steps):
     b = hc.Batch(ctx, precision="f32", max_slots=len(probs), **scheme)
     try:
@@ -118,3 +125,17 @@ def test_march_against_oracle(hc, ctx):
     ref = o.get_interior()
     l1 = float(np.mean(np.abs(got[:, 0] - ref[:, 0])))
     assert l1 <= 1e-5, l1
+
+
+@pytest.mark.parametrize("seg", ["0", "1", "5", "23"])
+def test_march_segment_lengths(hc, ctx, monkeypatch, seg):
+    """Segments shorter than the schedule's (0: the balanced length the batch
+    picks for a launch that would leave warps idle, here a few rows) give the
+    same bits as the tile kernel."""
+    monkeypatch.setenv("HC_MARCH_SEGMENT", seg)
+    probs = [_quad(hc, nx, ny, 95 + k) for k, (nx, ny) in enumerate([(61, 63), (150, 129), (31, 5), (2, 2)])]
+    scheme = dict(usePLM="plm cons", slopeLimiter="van Leer (abs)", integrator="Runge-Kutta 3, TVD")
+    a = _run(hc, ctx, probs, scheme, 17, 5)
+    b = _run(hc, ctx, probs, scheme, TILE, 5)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)

@@ -17,6 +17,13 @@ MARCH = 7       # 12 warps, segments of 32 planes
 TILE = 0        # the 3D tile schedule with every compiled-in limiter
 
 
+@pytest.fixture(autouse=True)
+def full_segments(monkeypatch):
+    """The schedule's own segment length: these small batches would otherwise
+    be cut into short balanced segments (tested on their own below)."""
+    monkeypatch.setenv("HC_MARCH_SEGMENT", "100000")
+
+
 def _run(hc, ctx, probs, scheme, schedule, steps):
     b = hc.Batch(ctx, precision="f32", max_slots=len(probs), **scheme)
     try:
@@ -129,3 +136,17 @@ def test_march3_against_oracle(hc, ctx):
         o.update()
     l1 = float(np.mean(np.abs(got[:, 0] - o.get_interior()[:, 0])))
     assert l1 <= 1e-5, l1
+
+
+@pytest.mark.parametrize("seg", ["0", "1", "6", "19"])
+def test_march3_segment_lengths(hc, ctx, monkeypatch, seg):
+    """Segments shorter than the schedule's (0: the balanced length the batch
+    picks for a launch that would leave CTAs idle, here a few planes) give
+    the same bits as the tile kernel."""
+    monkeypatch.setenv("HC_MARCH_SEGMENT", seg)
+    probs = [_blast(hc, *s) for s in [(31, 21, 65), (12, 10, 14), (2, 2, 2)]]
+    scheme = dict(usePLM="plm cons", slopeLimiter="minmod", integrator="Runge-Kutta 3, TVD")
+    a = _run(hc, ctx, probs, scheme, 10, 4)
+    b = _run(hc, ctx, probs, scheme, TILE, 4)
+    for k, (x, y) in enumerate(zip(a, b)):
+        _same(x, y, k)

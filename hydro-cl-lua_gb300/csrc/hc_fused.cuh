@@ -1316,30 +1316,75 @@ __global__ void k_calc_dt(const DevInst* inst, DevCtl* ctl, int slot, int buf) {
         atomicMin(&ctl[slot].dtmin[ctl[slot].par], (unsigned long long)__double_as_longlong(m));
 }
 
-// Interior <-> staging transfer with layout conversion (dir 0: staging -> grid).
+// Interior <-> staging transfer with layout conversion (dir 0: staging -> grid)
+// of interior cell k of n.
+template <typename T, int DIM>
+__device__ __forceinline__ void xferCell(const DevInst& I, T* base, void* staging, int layout, int dir, long long n,
+                                         long long k) {
+    int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
+    long long const idx = padIndex<DIM>(I, gx, gy, gz);
+    for (int f = 0; f < 5; ++f) {
+        T* g = base + f * I.plane + idx;
+        if (layout == HC_LAYOUT_AOS6_F64) {
+            double* h = (double*)staging + 6 * k + f;
+            if (dir == 0) *g = (T)*h; else *h = (double)*g;
+        } else if (layout == HC_LAYOUT_SOA5_F64) {
+            double* h = (double*)staging + f * n + k;
+            if (dir == 0) *g = (T)*h; else *h = (double)*g;
+        } else {
+            float* h = (float*)staging + f * n + k;
+            if (dir == 0) *g = (T)*h; else *h = (float)*g;
+        }
+    }
+    if (layout == HC_LAYOUT_AOS6_F64 && dir == 1) ((double*)staging)[6 * k + 5] = 0.;
+}
+
 template <typename T, int DIM>
 __global__ void k_xfer(const DevInst* inst, int slot, int buf, void* staging, int layout, int dir) {
     const DevInst& I = inst[slot];
     T* base = reinterpret_cast<T*>(I.buf[buf]);
     long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
-    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-        int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
-        long long const idx = padIndex<DIM>(I, gx, gy, gz);
-        for (int f = 0; f < 5; ++f) {
-            T* g = base + f * I.plane + idx;
-            if (layout == HC_LAYOUT_AOS6_F64) {
-                double* h = (double*)staging + 6 * k + f;
-                if (dir == 0) *g = (T)*h; else *h = (double)*g;
-            } else if (layout == HC_LAYOUT_SOA5_F64) {
-                double* h = (double*)staging + f * n + k;
-                if (dir == 0) *g = (T)*h; else *h = (double)*g;
-            } else {
-                float* h = (float*)staging + f * n + k;
-                if (dir == 0) *g = (T)*h; else *h = (float)*g;
-            }
-        }
-        if (layout == HC_LAYOUT_AOS6_F64 && dir == 1) ((double*)staging)[6 * k + 5] = 0.;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        xferCell<T, DIM>(I, base, staging, layout, dir, n, k);
+}
+
+// The instances of one batched set-up or gather launch: job j is state
+// buffer buf[j] of instance slot[j] with host-side buffer host[j] (page-locked
+// memory mapped for the device, or staging), worked on by blocks first[j] ..
+// first[j+1]-1, each taking kJobCells consecutive interior cells.  Passed by
+// value (under 4 KB).
+constexpr int kXferJobs = 120;
+constexpr int kJobCells = 1024;
+struct XferJobs {
+    int n;
+    int slot[kXferJobs];
+    int buf[kXferJobs];
+    int first[kXferJobs + 1];
+    void* host[kXferJobs];
+};
+
+// The job of block b: the last j with first[j] <= b.
+__device__ __forceinline__ int jobOf(const XferJobs& J, int b) {
+    int lo = 0, hi = J.n - 1;
+    while (lo < hi) {
+        int const mid = (lo + hi + 1) >> 1;
+        if (J.first[mid] <= b) lo = mid;
+        else hi = mid - 1;
     }
+    return lo;
+}
+
+// k_xfer over the instances of J, one launch: block b moves kJobCells cells of
+// its job (the same per-cell transfer).
+template <typename T, int DIM>
+__global__ void k_xfer_many(const DevInst* inst, const __grid_constant__ XferJobs J, int layout, int dir) {
+    int const j = jobOf(J, blockIdx.x);
+    const DevInst& I = inst[J.slot[j]];
+    T* base = reinterpret_cast<T*>(I.buf[J.buf[j]]);
+    long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
+    long long const k0 = (long long)(blockIdx.x - J.first[j]) * kJobCells;
+    long long const k1 = k0 + kJobCells < n ? k0 + kJobCells : n;
+    for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x) xferCell<T, DIM>(I, base, J.host[j], layout, dir, n, k);
 }
 
 // The two layers next to face (axis, side) of one slot's buffer, as AoS-6
@@ -1378,6 +1423,34 @@ __global__ void k_slab(const DevInst* inst, int slot, int buf, int axis, int sid
 // Every step reads and writes only its own cell's values, so the result is
 // that of k_xfer, k_constrain, k_fill_ghosts and k_calc_dt run in turn; the
 // linear / quadratic ghosts (k_extrap_slot) read neighbours and follow it.
+// One cell of the set-up pass (interior cell k of n); returns its CFL dt.
+template <typename T, int DIM, bool EXACT>
+__device__ __forceinline__ double loadCell(const DevInst& I, const TileK<T>& K, T* base, const void* staging,
+                                           int layout, int reset, long long n, long long k) {
+    int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
+    long long const idx = padIndex<DIM>(I, gx, gy, gz);
+    T u[5];
+    for (int f = 0; f < 5; ++f) {
+        if (layout == HC_LAYOUT_AOS6_F64) u[f] = (T)((const double*)staging)[6 * k + f];
+        else if (layout == HC_LAYOUT_SOA5_F64) u[f] = (T)((const double*)staging)[f * n + k];
+        else u[f] = (T)((const float*)staging)[f * n + k];
+    }
+    if (reset) constrainCell<T, EXACT>(u, K);
+    for (int f = 0; f < 5; ++f) base[f * I.plane + idx] = u[f];
+    bool edge = false;
+    int const g[3] = {gx, gy, gz};
+    for (int d = 0; d < DIM; ++d) edge |= g[d] < 2 || g[d] >= I.n[d] - 2;
+    if (edge) scatterGhosts<T, DIM>(I, base, gx, gy, gz, u);
+    return (double)dtCell<T, EXACT, DIM>(u, K, I);
+}
+
+// The warps' CFL minima into the slot's dtmin[par].
+__device__ __forceinline__ void dtminToSlot(DevCtl* ctl, int slot, double m) {
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m < __longlong_as_double((long long)kInfBits))
+        atomicMin(&ctl[slot].dtmin[ctl[slot].par], (unsigned long long)__double_as_longlong(m));
+}
+
 template <typename T, int DIM, bool EXACT>
 __global__ void k_load_state(const DevInst* inst, DevCtl* ctl, int slot, int buf, const void* staging, int layout,
                              int reset) {
@@ -1387,26 +1460,29 @@ __global__ void k_load_state(const DevInst* inst, DevCtl* ctl, int slot, int buf
     T* base = reinterpret_cast<T*>(I.buf[buf]);
     long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
     double m = __longlong_as_double((long long)kInfBits);
-    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-        int const gx = (int)(k % I.n[0]), gy = (int)((k / I.n[0]) % I.n[1]), gz = (int)(k / ((long long)I.n[0] * I.n[1]));
-        long long const idx = padIndex<DIM>(I, gx, gy, gz);
-        T u[5];
-        for (int f = 0; f < 5; ++f) {
-            if (layout == HC_LAYOUT_AOS6_F64) u[f] = (T)((const double*)staging)[6 * k + f];
-            else if (layout == HC_LAYOUT_SOA5_F64) u[f] = (T)((const double*)staging)[f * n + k];
-            else u[f] = (T)((const float*)staging)[f * n + k];
-        }
-        if (reset) constrainCell<T, EXACT>(u, K);
-        for (int f = 0; f < 5; ++f) base[f * I.plane + idx] = u[f];
-        bool edge = false;
-        int const g[3] = {gx, gy, gz};
-        for (int d = 0; d < DIM; ++d) edge |= g[d] < 2 || g[d] >= I.n[d] - 2;
-        if (edge) scatterGhosts<T, DIM>(I, base, gx, gy, gz, u);
-        m = fmin(m, (double)dtCell<T, EXACT, DIM>(u, K, I));
-    }
-    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0 && m < __longlong_as_double((long long)kInfBits))
-        atomicMin(&ctl[slot].dtmin[ctl[slot].par], (unsigned long long)__double_as_longlong(m));
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        m = fmin(m, loadCell<T, DIM, EXACT>(I, K, base, staging, layout, reset, n, k));
+    dtminToSlot(ctl, slot, m);
+}
+
+// k_load_state over the instances of J, one launch: block b sets up
+// kJobCells cells of its job (the same per-cell pass).
+template <typename T, int DIM, bool EXACT>
+__global__ void k_load_many(const DevInst* inst, DevCtl* ctl, const __grid_constant__ XferJobs J, int layout,
+                            int reset) {
+    int const j = jobOf(J, blockIdx.x);
+    int const slot = J.slot[j];
+    const DevInst& I = inst[slot];
+    TileK<T> K;
+    makeTileK<T>(K, I, nullptr, nullptr, 0, 0);
+    T* base = reinterpret_cast<T*>(I.buf[J.buf[j]]);
+    long long const n = (long long)I.n[0] * I.n[1] * I.n[2];
+    long long const k0 = (long long)(blockIdx.x - J.first[j]) * kJobCells;
+    long long const k1 = k0 + kJobCells < n ? k0 + kJobCells : n;
+    double m = __longlong_as_double((long long)kInfBits);
+    for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x)
+        m = fmin(m, loadCell<T, DIM, EXACT>(I, K, base, J.host[j], layout, reset, n, k));
+    dtminToSlot(ctl, slot, m);
 }
 
 // Kahan-compensated FP64 sums of the 5 fields times the cell volume; one
@@ -1477,6 +1553,9 @@ struct AuxLauncher {
     // k_load_state over `cells` interior cells
     void (*load)(const DevInst* inst, DevCtl* ctl, int slot, int buf, const void* staging, int layout, int reset,
                  long long cells, cudaStream_t s);
+    // k_load_many / k_xfer_many over the jobs of J (J.first[J.n] blocks)
+    void (*load_many)(const DevInst* inst, DevCtl* ctl, const XferJobs& J, int layout, int reset, cudaStream_t s);
+    void (*xfer_many)(const DevInst* inst, const XferJobs& J, int layout, int dir, cudaStream_t s);
     void (*extrap_slot)(const DevInst* inst, int slot, int buf, cudaStream_t s);
     void (*sums)(const DevInst* inst, int slot, int buf, double vol, double* partial, int blocks, cudaStream_t s);
     // linear / quadratic ghosts of a stage's output on every stepping instance of this dimension

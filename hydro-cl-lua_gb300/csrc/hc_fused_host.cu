@@ -529,7 +529,7 @@ int fused_reserve_staging(FusedSet* f, size_t bytes) { return ensure_staging(f, 
 // stream), its descriptor and control block in the pinned mirrors and its
 // tensor maps; uploading them is the caller's (upload_slots).
 static int add_host(FusedSet* f, int slot, const hc_solver_desc& d, double t_end, long long max_steps,
-                    int stop_on_error) {
+                    int stop_on_error, bool zero = true) {
     if (slot < 0 || slot >= f->max_slots || f->slots[slot].used) return fail(HC_ERR_STATE, "slot unavailable");
     HC_CHECK(validate(f, d));
     Slot& S = f->slots[slot];
@@ -543,7 +543,7 @@ static int add_host(FusedSet* f, int slot, const hc_solver_desc& d, double t_end
     S.bytes = planeBytes * 5 * (nb + nd);
     cudaError_t e = f->pool.alloc(S.bytes, &S.mem);
     if (e != cudaSuccess) { S.mem = nullptr; return cuda_fail(e, "cudaMalloc (instance state)"); }
-    HC_CUDA(cudaMemsetAsync(S.mem, 0, S.bytes, f->stream));
+    if (zero) HC_CUDA(cudaMemsetAsync(S.mem, 0, S.bytes, f->stream));
     DevInst& I = S.inst;
     std::memset(&I, 0, sizeof(I));
     I.dim = d.dim;
@@ -655,19 +655,52 @@ static void* pinned_device_ptr(const void* host) {
 // in place and otherwise its own range of one staging buffer, all queued back
 // to back (no wait).  Stops at the first instance the host side refuses;
 // *n_done = the instances admitted.
-int fused_add_many(FusedSet* f, int n, const int* slots, const hc_solver_desc* descs, const void* const* hosts,
-                   int layout, const double* t_end, const long long* max_steps, int stop_on_error, int* n_done) {
-    *n_done = 0;
-    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
-    int r = HC_OK;
-    int k = 0;
-    for (; k < n; ++k) {
-        r = add_host(f, slots[k], descs[k], t_end[k], max_steps[k], stop_on_error);
-        if (r != HC_OK) break;
+// Batched set-up (load) or gather passes over n instances: one launch per
+// grid dimension and kXferJobs instances; job j moves state buffer bufs[j] of
+// slots[j] from / to hosts[j].
+static void run_jobs(FusedSet* f, int n, const int* slots, const int* bufs, void* const* hosts, int layout, bool load) {
+    for (int dim = 1; dim <= 3; ++dim) {
+        const AuxLauncher* A = find_aux(f->sch.precision, dim);
+        fz::XferJobs J;
+        J.n = 0;
+        J.first[0] = 0;
+        auto flush = [&]() {
+            if (!J.n) return;
+            if (load) A->load_many(f->d_inst, f->d_ctl, J, layout, 1, f->stream);
+            else A->xfer_many(f->d_inst, J, layout, 1, f->stream);
+            J.n = 0;
+        };
+        for (int j = 0; j < n; ++j) {
+            const Slot& S = f->slots[slots[j]];
+            if (S.dim != dim) continue;
+            J.slot[J.n] = slots[j];
+            J.buf[J.n] = bufs[j];
+            J.host[J.n] = hosts[j];
+            J.first[J.n + 1] = J.first[J.n] + (int)((S.cells + fz::kJobCells - 1) / fz::kJobCells);
+            if (++J.n == fz::kXferJobs) flush();
+        }
+        flush();
     }
-    int const done = k;
-    *n_done = done;
-    if (!done) return r;
+}
+
+// The device side of admitting `done` instances whose host side add_host has
+// set up (zeroing not yet done): memory zeroed, descriptors uploaded, state
+// set up from hosts[j].
+static int setup_many(FusedSet* f, int done, const int* slots, const void* const* hosts, int layout) {
+    {
+        // the instances' memory zeroed: one memset per run of adjacent pool ranges
+        std::vector<std::pair<char*, size_t>> ranges(done);
+        for (int j = 0; j < done; ++j) ranges[j] = {(char*)f->slots[slots[j]].mem, f->slots[slots[j]].bytes};
+        std::sort(ranges.begin(), ranges.end());
+        for (size_t a = 0; a < ranges.size();) {
+            char* const lo = ranges[a].first;
+            char* hi = lo + ranges[a].second;
+            size_t b = a + 1;
+            while (b < ranges.size() && ranges[b].first == hi) hi += ranges[b++].second;
+            HC_CUDA(cudaMemsetAsync(lo, 0, (size_t)(hi - lo), f->stream));
+            a = b;
+        }
+    }
     std::vector<int> sorted(slots, slots + done);
     std::sort(sorted.begin(), sorted.end());
     for (size_t a = 0; a < sorted.size();) {
@@ -683,20 +716,49 @@ int fused_add_many(FusedSet* f, int n, const int* slots, const hc_solver_desc* d
         off[j + 1] = off[j] + (direct[j] ? 0 : round_up(layout_bytes(f->slots[slots[j]].cells, layout), 256));
     }
     if (off[done]) HC_CHECK(ensure_staging(f, off[done]));
+    // fixed ghosts first, then the set-up passes, then the linear / quadratic
+    // ghosts (which read the interior)
+    std::vector<void*> src(done);
     for (int j = 0; j < done; ++j) {
         Slot& S = f->slots[slots[j]];
-        const AuxLauncher* A = find_aux(f->sch.precision, S.dim);
-        if (has_fixed(S)) A->fixed_ghosts(f->d_inst, slots[j], f->plan[0].n_state_bufs, f->stream);
-        void* src = direct[j];
-        if (!src) {
-            src = static_cast<char*>(f->staging) + off[j];
-            HC_CUDA(cudaMemcpyAsync(src, hosts[j], layout_bytes(S.cells, layout), cudaMemcpyHostToDevice, f->stream));
+        if (has_fixed(S)) find_aux(f->sch.precision, S.dim)->fixed_ghosts(f->d_inst, slots[j], f->plan[0].n_state_bufs,
+                                                                         f->stream);
+        src[j] = direct[j];
+        if (!src[j]) {
+            src[j] = static_cast<char*>(f->staging) + off[j];
+            HC_CUDA(cudaMemcpyAsync(src[j], hosts[j], layout_bytes(S.cells, layout), cudaMemcpyHostToDevice, f->stream));
         }
-        A->load(f->d_inst, f->d_ctl, slots[j], 0, src, layout, 1, S.cells, f->stream);
-        if (has_extrap(S)) A->extrap_slot(f->d_inst, slots[j], 0, f->stream);
+    }
+    std::vector<int> bufs(done, 0);
+    run_jobs(f, done, slots, bufs.data(), src.data(), layout, true);
+    for (int j = 0; j < done; ++j) {
+        Slot& S = f->slots[slots[j]];
+        if (has_extrap(S)) find_aux(f->sch.precision, S.dim)->extrap_slot(f->d_inst, slots[j], 0, f->stream);
     }
     HC_CUDA(cudaGetLastError());
-    f->items_dirty = true;
+    return HC_OK;
+}
+
+int fused_add_many(FusedSet* f, int n, const int* slots, const hc_solver_desc* descs, const void* const* hosts,
+                   int layout, const double* t_end, const long long* max_steps, int stop_on_error, int* n_done) {
+    *n_done = 0;
+    if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
+    int r = HC_OK;
+    int k = 0;
+    // in chunks of one set-up launch's instances: the device sets up a chunk
+    // while the host prepares the next
+    while (k < n && r == HC_OK) {
+        int const k0 = k, end = std::min(n, k0 + fz::kXferJobs);
+        for (; k < end; ++k) {
+            r = add_host(f, slots[k], descs[k], t_end[k], max_steps[k], stop_on_error, false);
+            if (r != HC_OK) break;
+        }
+        *n_done = k;
+        if (k > k0) {
+            f->items_dirty = true;
+            HC_CHECK(setup_many(f, k - k0, slots + k0, hosts + k0, layout));
+        }
+    }
     return r;
 }
 
@@ -715,12 +777,13 @@ int fused_get_state_many(FusedSet* f, int n, const int* slots, void* const* host
         off[j + 1] = off[j] + (direct[j] ? 0 : round_up(layout_bytes(S.cells, layout), 256));
     }
     if (off[n]) HC_CHECK(ensure_staging(f, off[n]));
+    std::vector<void*> dst(n);
+    std::vector<int> bufs(n);
     for (int j = 0; j < n; ++j) {
-        const Slot& S = f->slots[slots[j]];
-        void* const dst = direct[j] ? direct[j] : static_cast<char*>(f->staging) + off[j];
-        find_aux(f->sch.precision, S.dim)->xfer(f->d_inst, slots[j], state_buf(f, slots[j]), dst, layout, 1, S.cells,
-                                                 f->stream);
+        dst[j] = direct[j] ? direct[j] : static_cast<char*>(f->staging) + off[j];
+        bufs[j] = state_buf(f, slots[j]);
     }
+    run_jobs(f, n, slots, bufs.data(), dst.data(), layout, false);
     HC_CUDA(cudaGetLastError());
     for (int j = 0; j < n; ++j)
         if (!direct[j])
@@ -1329,7 +1392,9 @@ int fused_autotune_keep(FusedSet* f, int slot, const char* cache_path) {
 }
 
 int fused_set_schedule(FusedSet* f, int dim, int variant) {
-    if (!find_launcher(f->sch, dim, variant)) return fail(HC_ERR_INVALID, "no such schedule for this scheme and dimension");
+    const StageLauncher* L = find_launcher(f->sch, dim, variant);
+    if (!L) return fail(HC_ERR_INVALID, "no such schedule for this scheme and dimension");
+    if (f->launcher[dim - 1] == L) return HC_OK;   // already running it (its maps encoded for it)
     HC_CUDA(cudaStreamSynchronize(f->stream));
     HC_CHECK(set_launcher(f, dim, variant));
     reencode_all(f, dim);

@@ -217,6 +217,12 @@ void add_aux(std::vector<AuxLauncher>& v) {
                 long long cells, cudaStream_t s) {
         k_load_state<T, DIM, EXACT><<<gridFor(cells), 256, 0, s>>>(inst, ctl, slot, buf, staging, layout, reset);
     };
+    a.load_many = [](const DevInst* inst, DevCtl* ctl, const XferJobs& J, int layout, int reset, cudaStream_t s) {
+        k_load_many<T, DIM, EXACT><<<(unsigned)J.first[J.n], 256, 0, s>>>(inst, ctl, J, layout, reset);
+    };
+    a.xfer_many = [](const DevInst* inst, const XferJobs& J, int layout, int dir, cudaStream_t s) {
+        k_xfer_many<T, DIM><<<(unsigned)J.first[J.n], 256, 0, s>>>(inst, J, layout, dir);
+    };
     a.extrap_slot = [](const DevInst* inst, int slot, int buf, cudaStream_t s) {
         k_extrap_slot<T, DIM><<<64, 256, 0, s>>>(inst, slot, buf);
     };

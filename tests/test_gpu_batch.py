@@ -278,6 +278,45 @@ def test_admit_many_and_fetch_many_same_bits_as_one_by_one(hc, ctx, layout):
         L.hc_host_free(ptr)
 
 
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_admit_many_fetch_many_mixed_dims_several_launches(hc, ctx, precision):
+    """More instances of one dimension than one batched set-up launch takes
+    (120), beside 1D and 3D ones, admitted and fetched in one call each: the
+    same bits as one-at-a-time admission and fetch, for each layout."""
+    probs = []
+    for k in range(125):
+        a = cases.c4_quadrant(6 + k % 23)
+        probs.append((a, hc.quadrant_state(a, hc.random_quadrants(hc.SplitMix64(300 + k)))))
+    for n in (40, 77, 130):
+        a = dict(cases.c1_sod(gridSize=n, fluxLimiter="donor cell"), **SCHEME)
+        probs.append((a, hc.sod_state(a)))
+    for n in (6, 11):
+        a = dict(cases.c3_blast(n), **SCHEME)
+        probs.append((a, hc.blast_state(a)))
+    for layout in ("aos6", "soa5"):
+        conv = (lambda c: c) if layout == "aos6" else \
+            (lambda c: np.ascontiguousarray(c.reshape(-1, 6)[:, :5].T))
+        got = {}
+        for form in ("one", "many"):
+            b = hc.Batch(ctx, precision=precision, max_slots=len(probs), **SCHEME)
+            try:
+                if form == "one":
+                    slots = [b.admit(a, conv(u), np.inf, max_steps=3, tag=k, layout=layout)
+                             for k, (a, u) in enumerate(probs)]
+                else:
+                    slots = b.admit_many([(a, conv(u), np.inf, 3, k) for k, (a, u) in enumerate(probs)],
+                                         layout=layout)
+                b.step(3)
+                if form == "one":
+                    got[form] = [b.fetch(s, layout) for s in slots]
+                else:
+                    got[form] = b.fetch_many(slots, layout, [np.empty_like(conv(u)) for _, u in probs])
+            finally:
+                b.close()
+        for k, (x, y) in enumerate(zip(got["one"], got["many"])):
+            np.testing.assert_array_equal(np.asarray(x).reshape(y.shape), y, err_msg="%s instance %d" % (layout, k))
+
+
 def test_admit_many_stops_at_the_first_refusal(hc, ctx):
     """A refusal inside admit_many leaves the instances before it admitted
     (reported in the error's .slots) and admits none after it."""

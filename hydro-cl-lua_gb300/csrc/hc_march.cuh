@@ -67,6 +67,8 @@ inline int marchEpi(const StageDev& s) {
 // The y axis' interface frame takes (rho, m.y, m.z, m.x, E): global field g of
 // the y lane sits at frame index kYFrame[g].
 __device__ __forceinline__ constexpr int yFrameOf(int g) { return g == 0 ? 0 : (g == 4 ? 4 : (g == 1 ? 3 : g - 1)); }
+// and frame index j holds global field yGlobalOf(j)
+__device__ __forceinline__ constexpr int yGlobalOf(int j) { return j == 0 ? 0 : (j == 4 ? 4 : (j == 3 ? 1 : j + 1)); }
 
 // The ghost copies a finished 2D cell (x, y) at padded index idx makes
 // (gridsolver.lua:638-780): periodic wraps, mirror reflects with the normal
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
 
         // carried by the march (the cells themselves are re-read from shared
         // memory, which holds rows r-1 .. r+1 at every step)
-        float Ry[5];       // the y-side R state of cell (x, r-1), global frame
+        float Ry[5];       // the y-side R state of cell (x, r-1), y interface frame
         float Fyp[5];      // the y flux at the lower face of cell (x, r-1), global frame
         float Dxp[5];      // the x flux difference of cell (x, r-1)
 #pragma unroll
@@ -255,30 +257,29 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
             const float* const rm = wb + ((ir - 1) / C % NB) * Cfg::BUFF + ((ir - 1) % C) * kMarchBW + col;
             const float* const r0 = wb + (ir / C % NB) * Cfg::BUFF + (ir % C) * kMarchBW + col;
             const float* const rp = wb + ((ir + 1) / C % NB) * Cfg::BUFF + ((ir + 1) % C) * kMarchBW + col;
-            // x and y half slopes of (x, r): L = U - h, R = U + h
+            // x and y half slopes of (x, r), L = U - h, R = U + h, paired in
+            // the interface frames: pair j holds global field j on the x axis
+            // and field yGlobalOf(j) on the y axis, as the Roe lanes take them
             float2 L[5], R[5];
 #pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                float const u0 = r0[f * C * kMarchBW];
-                float2 const c = make_float2(u0, u0);
-                float2 const dL = lanes::sub(c, make_float2(r0[f * C * kMarchBW - 1], rm[f * C * kMarchBW]));
-                float2 const dR = lanes::sub(make_float2(r0[f * C * kMarchBW + 1], rp[f * C * kMarchBW]), c);
+            for (int j = 0; j < 5; ++j) {
+                int const g = yGlobalOf(j);
+                float2 const c = make_float2(r0[j * C * kMarchBW], r0[g * C * kMarchBW]);
+                float2 const dL = lanes::sub(c, make_float2(r0[j * C * kMarchBW - 1], rm[g * C * kMarchBW]));
+                float2 const dR = lanes::sub(make_float2(r0[j * C * kMarchBW + 1], rp[g * C * kMarchBW]), c);
                 float2 const h = lanes::halfSlope<SLOPE>(dL, dR, slim);
-                L[f] = lanes::sub(c, h);
-                R[f] = lanes::add(c, h);
+                L[j] = lanes::sub(c, h);
+                R[j] = lanes::add(c, h);
             }
             if (ir >= 2) {
                 // faces: x (left neighbour's R | own L), y (own R one row down | own L)
                 lanes::C5<float2> UL, UR;
 #pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    float const rxl = __shfl_up_sync(FULL, R[f].x, 1);
-                    int const j = yFrameOf(f);
-                    // frame index j of the x lane is global field j; of the y lane, global field f
-                    UL.u[f].x = rxl;
-                    UR.u[f].x = L[f].x;
-                    UL.u[j].y = Ry[f];
-                    UR.u[j].y = L[f].y;
+                for (int j = 0; j < 5; ++j) {
+                    UL.u[j].x = __shfl_up_sync(FULL, R[j].x, 1);
+                    UR.u[j].x = L[j].x;
+                    UL.u[j].y = Ry[j];
+                    UR.u[j].y = L[j].y;
                 }
                 float2 F[5];
                 bool const plain = lanes::roeUp2(F, le, UL, UR);
@@ -419,7 +420,7 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                 }
             }
 #pragma unroll
-            for (int f = 0; f < 5; ++f) Ry[f] = R[f].y;
+            for (int j = 0; j < 5; ++j) Ry[j] = R[j].y;
         }
         if (timedOut) return;
         // one FP64 atomicMin per item for the next step's CFL dt

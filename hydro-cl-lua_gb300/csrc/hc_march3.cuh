@@ -57,6 +57,8 @@ struct March3Cfg {
 // The z axis' interface frame takes (rho, m.z, m.x, m.y, E): global field g of
 // the z lane sits at frame index zFrameOf(g).
 __device__ __forceinline__ constexpr int zFrameOf(int g) { return g == 0 ? 0 : (g == 4 ? 4 : (g == 3 ? 1 : g + 1)); }
+// and frame index j holds global field zGlobalOf(j)
+__device__ __forceinline__ constexpr int zGlobalOf(int j) { return j == 0 ? 0 : (j == 4 ? 4 : (j == 1 ? 3 : j - 1)); }
 
 // The z ghost copies of a finished 3D cell at plane z, padded index idx (a
 // plane is s elements): those of scatterGhosts along z.
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
         bool const edgeXY = x0 < 2 || x0 + kStripW > nx - 2 || yw < 2 || yw >= ny - 2;
 
         // carried by the march
-        float Rz[5];       // the z-side R state of the cell below (plane p-1)
+        float Rz[5];       // the z-side R state of the cell below (plane p-1), z interface frame
         float Fzp[5];      // the z flux at the lower face of the cell below
         float Dxy[5];      // the x and y flux differences of the cell below
 #pragma unroll
@@ -220,9 +222,10 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
             const float* const pm = ring + ((iz - 1) % NB) * Cfg::BUFF + cell;
             const float* const p0 = ring + (iz % NB) * Cfg::BUFF + cell;
             const float* const pp = ring + ((iz + 1) % NB) * Cfg::BUFF + cell;
-            // half slopes, L = U - h, R = U + h: x and z of the tile rows'
-            // cells on register pairs (.x: x axis, .y: z axis); y of the
-            // row's cell (its R) and of the cell above (its L)
+            // half slopes, L = U - h, R = U + h: y of the row's cell (its R)
+            // and of the cell above (its L); x and z of the tile rows' cells
+            // on register pairs in the interface frames (pair j: global field
+            // j on the x axis, field zGlobalOf(j) on the z axis)
             float2 Lxz[5], Rxz[5];
             float Ry[5], Lya[5];
             if (faceRow) {
@@ -236,13 +239,17 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                                                               lanes::sub(p0[f * FS + 2 * kMarchBW], ua), slim);
                     Ry[f] = lanes::add(u0, hy);
                     Lya[f] = lanes::sub(ua, hya);
-                    if (tileRow) {
-                        float2 const c = make_float2(u0, u0);
-                        float2 const dL = lanes::sub(c, make_float2(p0[f * FS - 1], pm[f * FS]));
-                        float2 const dR = lanes::sub(make_float2(p0[f * FS + 1], pp[f * FS]), c);
+                }
+                if (tileRow) {
+#pragma unroll
+                    for (int j = 0; j < 5; ++j) {
+                        int const g = zGlobalOf(j);
+                        float2 const c = make_float2(p0[j * FS], p0[g * FS]);
+                        float2 const dL = lanes::sub(c, make_float2(p0[j * FS - 1], pm[g * FS]));
+                        float2 const dR = lanes::sub(make_float2(p0[j * FS + 1], pp[g * FS]), c);
                         float2 const h = lanes::halfSlope<SLOPE>(dL, dR, slim);
-                        Lxz[f] = lanes::sub(c, h);
-                        Rxz[f] = lanes::add(c, h);
+                        Lxz[j] = lanes::sub(c, h);
+                        Rxz[j] = lanes::add(c, h);
                     }
                 }
             }
@@ -272,13 +279,11 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                 // (the cell below's R | own L), on register pairs
                 lanes::C5<float2> UL, UR;
 #pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    float const rxl = __shfl_up_sync(FULL, Rxz[f].x, 1);
-                    int const j = zFrameOf(f);
-                    UL.u[f].x = rxl;
-                    UR.u[f].x = Lxz[f].x;
-                    UL.u[j].y = Rz[f];
-                    UR.u[j].y = Lxz[f].y;
+                for (int j = 0; j < 5; ++j) {
+                    UL.u[j].x = __shfl_up_sync(FULL, Rxz[j].x, 1);
+                    UR.u[j].x = Lxz[j].x;
+                    UL.u[j].y = Rz[j];
+                    UR.u[j].y = Lxz[j].y;
                 }
                 float2 F[5];
                 bool const plain = lanes::roeUp2(F, le, UL, UR);
@@ -435,7 +440,7 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
             }
             if (tileRow) {
 #pragma unroll
-                for (int f = 0; f < 5; ++f) Rz[f] = Rxz[f].y;
+                for (int j = 0; j < 5; ++j) Rz[j] = Rxz[j].y;
             }
         }
         if (timedOut) {

@@ -222,11 +222,8 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
             const float* const pm = ring + ((iz - 1) % NB) * Cfg::BUFF + cell;
             const float* const p0 = ring + (iz % NB) * Cfg::BUFF + cell;
             const float* const pp = ring + ((iz + 1) % NB) * Cfg::BUFF + cell;
-            // half slopes, L = U - h, R = U + h: y of the row's cell (its R)
-            // and of the cell above (its L); x and z of the tile rows' cells
-            // on register pairs in the interface frames (pair j: global field
-            // j on the x axis, field zGlobalOf(j) on the z axis)
-            float2 Lxz[5], Rxz[5];
+            // y half slopes, L = U - h, R = U + h: the row's cell (its R) and
+            // the cell above (its L)
             float Ry[5], Lya[5];
             if (faceRow) {
 #pragma unroll
@@ -239,18 +236,6 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                                                               lanes::sub(p0[f * FS + 2 * kMarchBW], ua), slim);
                     Ry[f] = lanes::add(u0, hy);
                     Lya[f] = lanes::sub(ua, hya);
-                }
-                if (tileRow) {
-#pragma unroll
-                    for (int j = 0; j < 5; ++j) {
-                        int const g = zGlobalOf(j);
-                        float2 const c = make_float2(p0[j * FS], p0[g * FS]);
-                        float2 const dL = lanes::sub(c, make_float2(p0[j * FS - 1], pm[g * FS]));
-                        float2 const dR = lanes::sub(make_float2(p0[j * FS + 1], pp[g * FS]), c);
-                        float2 const h = lanes::halfSlope<SLOPE>(dL, dR, slim);
-                        Lxz[j] = lanes::sub(c, h);
-                        Rxz[j] = lanes::add(c, h);
-                    }
                 }
             }
             float* const fyp = FY + (iz & 1) * Cfg::XCH;
@@ -274,7 +259,22 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                 }
             }
             float fx[5], fz[5];
-            if (iz >= 2 && tileRow) {
+            if (tileRow) {
+                // x and z half slopes of the cell, after the y face (fewer
+                // values live across it), on register pairs in the interface
+                // frames (pair j: global field j on the x axis, field
+                // zGlobalOf(j) on the z axis)
+                float2 Lxz[5], Rxz[5];
+#pragma unroll
+                for (int j = 0; j < 5; ++j) {
+                    int const g = zGlobalOf(j);
+                    float2 const c = make_float2(p0[j * FS], p0[g * FS]);
+                    float2 const dL = lanes::sub(c, make_float2(p0[j * FS - 1], pm[g * FS]));
+                    float2 const dR = lanes::sub(make_float2(p0[j * FS + 1], pp[g * FS]), c);
+                    float2 const h = lanes::halfSlope<SLOPE>(dL, dR, slim);
+                    Lxz[j] = lanes::sub(c, h);
+                    Rxz[j] = lanes::add(c, h);
+                }
                 // the left x face (left lane's R | own L) and the lower z face
                 // (the cell below's R | own L), on register pairs
                 lanes::C5<float2> UL, UR;
@@ -284,30 +284,33 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                     UR.u[j].x = Lxz[j].x;
                     UL.u[j].y = Rz[j];
                     UR.u[j].y = Lxz[j].y;
+                    Rz[j] = Rxz[j].y;   // the next plane's cell below
                 }
-                float2 F[5];
-                bool const plain = lanes::roeUp2(F, le, UL, UR);
-                if (!__all_sync(FULL, plain)) {
-                    // a lane has a vacuum side or a degenerate average: every
-                    // lane evaluates both faces in the scalar form
+                if (iz >= 2) {
+                    float2 F[5];
+                    bool const plain = lanes::roeUp2(F, le, UL, UR);
+                    if (!__all_sync(FULL, plain)) {
+                        // a lane has a vacuum side or a degenerate average: every
+                        // lane evaluates both faces in the scalar form
 #pragma unroll 1
-                    for (int k = 0; k < 2; ++k) {
-                        lanes::C5<float> l, r;
+                        for (int k = 0; k < 2; ++k) {
+                            lanes::C5<float> l, r;
 #pragma unroll
-                        for (int j = 0; j < 5; ++j) {
-                            l.u[j] = lanes::lane(UL.u[j], k);
-                            r.u[j] = lanes::lane(UR.u[j], k);
+                            for (int j = 0; j < 5; ++j) {
+                                l.u[j] = lanes::lane(UL.u[j], k);
+                                r.u[j] = lanes::lane(UR.u[j], k);
+                            }
+                            float fk[5];
+                            lanes::roe<float>(fk, le, l, r);
+#pragma unroll
+                            for (int j = 0; j < 5; ++j) lanes::setLane(F[j], k, fk[j]);
                         }
-                        float fk[5];
-                        lanes::roe<float>(fk, le, l, r);
-#pragma unroll
-                        for (int j = 0; j < 5; ++j) lanes::setLane(F[j], k, fk[j]);
                     }
-                }
 #pragma unroll
-                for (int f = 0; f < 5; ++f) {
-                    fx[f] = zeroX ? 0.f : F[f].x;
-                    fz[f] = zeroZ ? 0.f : F[zFrameOf(f)].y;
+                    for (int f = 0; f < 5; ++f) {
+                        fx[f] = zeroX ? 0.f : F[f].x;
+                        fz[f] = zeroZ ? 0.f : F[zFrameOf(f)].y;
+                    }
                 }
             }
             // the y face fluxes are published; a timed-out wait stops the CTA
@@ -437,10 +440,6 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                         if (inCols) dtmin = fast::tmin(dtmin, dtc);
                     }
                 }
-            }
-            if (tileRow) {
-#pragma unroll
-                for (int j = 0; j < 5; ++j) Rz[j] = Rxz[j].y;
             }
         }
         if (timedOut) {

@@ -385,14 +385,15 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                             }
                         }
                         if constexpr (EPI != 1) {
-                            if (yc + 1 < y0 + rows) {
+                            // the next row's cell (the segment's last row read
+                            // again at its end: no branch), and into L2 eight
+                            // rows ahead (the last row repeated near the end)
+                            const float* const pc = a0src + idx;
+                            const float* const pn = pc + (yc + 1 < y0 + rows ? geo.px : 0);
 #pragma unroll
-                                for (int f = 0; f < 5; ++f) pre[f] = a0src[f * geo.plane + idx + geo.px];
-                            }
-                            // and into L2 eight rows ahead (the last row of the
-                            // segment repeated near its end)
+                            for (int f = 0; f < 5; ++f) pre[f] = pn[f * geo.plane];
                             int const ahead = yc + 8 < y0 + rows ? 8 : y0 + rows - 1 - yc;
-                            const float* const pf = a0src + idx + (long long)ahead * geo.px;
+                            const float* const pf = pc + (long long)ahead * geo.px;
 #pragma unroll
                             for (int f = 0; f < 5; ++f)
                                 asm volatile("prefetch.global.L2 [%0];" ::"l"(pf + f * geo.plane));
@@ -411,7 +412,8 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                     }
                     // after constrainU a non-finite momentum shows in ETotal
                     bad |= inCols && !fast::M<float>::finite_(u[0] + u[4]);
-                    if (edgeX || yc < 2 || yc >= ny - 2)
+                    // the same for every lane: a warp-uniform branch
+                    if (__any_sync(FULL, edgeX || yc < 2 || yc >= ny - 2))
                         if (inCols) marchGhosts(out, geo.plane, geo.px, nx, ny, geo.bc, x, yc, idx, u);
                     if (st.last) {
                         float const dtc = lanes::dtCell<float, 2>(u, le, K.gdx);

@@ -352,9 +352,11 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                         for (int f = 0; f < 5; ++f) u[f] = lanes::fma(lanes::sub(w[f], p[f]), K.calpha[m], u[f]);
                     }
                     // the next step's cell
-                    if (a0 >= 0 && yc + 1 < y0 + rows) {
+                    if (a0 >= 0) {
+                        // (the segment's last row read again at its end: no branch)
+                        const float* const pn = a0src + idx + (yc + 1 < y0 + rows ? geo.px : 0);
 #pragma unroll
-                        for (int f = 0; f < 5; ++f) pre[f] = a0src[f * geo.plane + idx + geo.px];
+                        for (int f = 0; f < 5; ++f) pre[f] = pn[f * geo.plane];
                     }
 #pragma unroll
                     for (int m = 0; m < 4; ++m) {

@@ -54,12 +54,13 @@ struct MarchCfg {
 // structure at run time; the others have it fixed -- no stored derivatives
 // and no beta terms, a current-derivative term, and the alpha terms
 //   1: the staged input alone (forward Euler, the first stage of RK2 / RK3-TVD)
-//   2: one state from global memory (the midpoint RK2's second stage)
+//   2: one state from global memory, on the step's last stage (the midpoint
+//      RK2's second stage): the CFL dt without a run-time test
 //   3: one state from global memory, then the staged input (the later stages
 //      of RK2-TVD and RK3-TVD)
 inline int marchEpi(const StageDev& s) {
     if (s.n_beta != 0 || s.store_deriv >= 0 || s.beta_cur == 0.) return 0;
-    if (s.n_alpha == 1) return s.alpha_buf[0] == s.in_buf ? 1 : 2;
+    if (s.n_alpha == 1) return s.alpha_buf[0] == s.in_buf ? 1 : (s.last ? 2 : 0);
     if (s.n_alpha == 2 && s.alpha_buf[0] != s.in_buf && s.alpha_buf[1] == s.in_buf) return 3;
     return 0;
 }
@@ -417,7 +418,7 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                     // the same for every lane: a warp-uniform branch
                     if (__any_sync(FULL, edgeX || yc < 2 || yc >= ny - 2))
                         if (inCols) marchGhosts(out, geo.plane, geo.px, nx, ny, geo.bc, x, yc, idx, u);
-                    if (st.last) {
+                    if (EPI == 2 || st.last) {
                         float const dtc = lanes::dtCell<float, 2>(u, le, K.gdx);
                         if (inCols) dtmin = fast::tmin(dtmin, dtc);
                     }
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
         }
         if (timedOut) return;
         // one FP64 atomicMin per item for the next step's CFL dt
-        if (st.last) {
+        if (EPI == 2 || st.last) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) dtmin = fast::tmin(dtmin, __shfl_xor_sync(FULL, dtmin, o));
             double const m = (double)dtmin;

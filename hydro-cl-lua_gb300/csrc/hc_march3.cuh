@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                         if (edgeXY) marchGhosts(out, geo.plane, geo.px, nx, ny, geo.bc, x, yw, idx, u);
                         if (zc < 2 || zc >= nz - 2) marchGhostsZ(out, geo.plane, ps, nz, geo.bc, zc, idx, u);
                     }
-                    if (st.last) {
+                    if (EPI == 2 || st.last) {
                         float const dtc = lanes::dtCell<float, 3>(u, le, K.gdx);
                         if (inCols) dtmin = fast::tmin(dtmin, dtc);
                     }
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
             return;
         }
         // one FP64 atomicMin per warp and item for the next step's CFL dt
-        if (st.last && tileRow) {
+        if ((EPI == 2 || st.last) && tileRow) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) dtmin = fast::tmin(dtmin, __shfl_xor_sync(FULL, dtmin, o));
             double const m = (double)dtmin;

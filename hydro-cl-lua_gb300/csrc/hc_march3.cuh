@@ -405,14 +405,16 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                             }
                         }
                         if constexpr (EPI != 1) {
-                            if (zc + 1 < z0 + planes) {
+                            // the next plane's cell (the segment's last plane
+                            // read again at its end: no branch), and into L2
+                            // eight planes ahead (the last plane repeated near
+                            // the end)
+                            const float* const pc = a0src + idx;
+                            const float* const pn = pc + (zc + 1 < z0 + planes ? ps : 0);
 #pragma unroll
-                                for (int f = 0; f < 5; ++f) pre[f] = a0src[f * geo.plane + idx + ps];
-                            }
-                            // and into L2 eight planes ahead (the segment's
-                            // last plane repeated near its end)
+                            for (int f = 0; f < 5; ++f) pre[f] = pn[f * geo.plane];
                             int const ahead = zc + 8 < z0 + planes ? 8 : z0 + planes - 1 - zc;
-                            const float* const pf = a0src + idx + (long long)ahead * ps;
+                            const float* const pf = pc + (long long)ahead * ps;
 #pragma unroll
                             for (int f = 0; f < 5; ++f)
                                 asm volatile("prefetch.global.L2 [%0];" ::"l"(pf + f * geo.plane));

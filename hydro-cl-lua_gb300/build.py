@@ -44,6 +44,7 @@ SOURCES = {
     "hc_fused_f32_m2.cu": FAST,
     "hc_fused_f32_m3.cu": FAST,
     "hc_fused_f32_m2b.cu": FAST,
+    "hc_fused_f32_m2c.cu": FAST,
     "hc_probe.cu": [],
     "hc_fused_f64_d1.cu": EXACT,
     "hc_fused_f64_d2.cu": EXACT,

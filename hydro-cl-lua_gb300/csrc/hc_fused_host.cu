@@ -1421,6 +1421,7 @@ void register_f32_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_m2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_m3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f32_m2b(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
+void register_f32_m2c(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d1(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d2(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
 void register_f64_d3(std::vector<StageLauncher>&, std::vector<AuxLauncher>&);
@@ -1440,6 +1441,7 @@ void register_launchers(std::vector<StageLauncher>& st, std::vector<AuxLauncher>
     register_f32_m2(st, aux);
     register_f32_m3(st, aux);
     register_f32_m2b(st, aux);
+    register_f32_m2c(st, aux);
     register_f64_d1(st, aux);
     register_f64_d2(st, aux);
     register_f64_d3(st, aux);

@@ -102,9 +102,9 @@ def test_march_equals_tile_boundaries(hc, ctx, bi):
         np.testing.assert_array_equal(x, y)
 
 
-@pytest.mark.parametrize("schedule", [17, 18, 19, 20])
+@pytest.mark.parametrize("schedule", [17, 18, 19, 20, 21])
 def test_march_occupancy_variants(hc, ctx, schedule):
-    """The same kernel compiled for 3 and 2 CTAs per SM, and with segments of 16 and 32 rows."""
+    """The same kernel compiled for 3 and 2 CTAs per SM, and with segments of 16, 32 and 128 rows."""
     probs = [_quad(hc, nx, ny, 90 + k) for k, (nx, ny) in enumerate([(61, 63), (150, 129)])]
     scheme = dict(usePLM="plm cons", slopeLimiter="van Leer (abs)", integrator="Runge-Kutta 2")
     a = _run(hc, ctx, probs, scheme, schedule, 6)

@@ -818,15 +818,19 @@ static int march_segment(const FusedSet* f, int d) {
     int const full = L->seg;
     if (f->seg_fixed > 0) return std::min(f->seg_fixed, full);
     long long const units = (long long)f->grid[d] * (d == 1 ? L->nthreads / 32 : 1);
+    // per live instance: its strips (times its y tiles in 3D) and its extent
+    // along the marching axis
+    std::vector<std::pair<long long, int>> live;
+    for (int s = 0; s < f->max_slots; ++s) {
+        const Slot& S = f->slots[s];
+        if (!S.used || !f->h_ctl[s].active || S.dim != d + 1) continue;
+        long long const strips = (S.inst.n[0] + L->tx - 1) / L->tx;
+        long long const tiles = d == 2 ? (S.inst.n[1] + L->ty - 1) / L->ty : 1;
+        live.emplace_back(strips * tiles, S.inst.n[d]);
+    }
     auto count = [&](int h) {
         long long n = 0;
-        for (int s = 0; s < f->max_slots; ++s) {
-            const Slot& S = f->slots[s];
-            if (!S.used || !f->h_ctl[s].active || S.dim != d + 1) continue;
-            long long const strips = (S.inst.n[0] + L->tx - 1) / L->tx;
-            long long const tiles = d == 2 ? (S.inst.n[1] + L->ty - 1) / L->ty : 1;
-            n += strips * tiles * ((S.inst.n[d] + h - 1) / h);
-        }
+        for (const auto& v : live) n += v.first * ((v.second + h - 1) / h);
         return n;
     };
     long long const nfull = count(full);

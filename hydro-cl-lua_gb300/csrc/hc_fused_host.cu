@@ -1343,8 +1343,9 @@ int fused_autotune(FusedSet* f, const char* cache_path) {
             HC_CUDA(cudaStreamSynchronize(f->stream));
             const StageLauncher* Lc = f->launcher[dim - 1];
             log << "# " << key << " variant " << v << " tile " << Lc->tx << "x" << Lc->ty << "x" << Lc->tz << " threads "
-                << Lc->nthreads << " seg " << Lc->seg << " (items: " << f->seg[dim - 1] << ") unroll " << Lc->unroll
-                << " ctas/SM " << Lc->min_ctas
+                << Lc->nthreads << " seg " << Lc->seg;
+            if (Lc->march) log << " (items: " << f->seg[dim - 1] << ")";
+            log << " unroll " << Lc->unroll << " ctas/SM " << Lc->min_ctas
                 << " lanes " << Lc->lanes << " slope " << Lc->slope << " ms/step " << ms / reps << "\n";
             if (ms < bestMs) { bestMs = ms; best = v; }
         }

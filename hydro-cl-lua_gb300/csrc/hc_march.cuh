@@ -302,16 +302,15 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                         for (int j = 0; j < 5; ++j) lanes::setLane(F[j], k, fk[j]);
                     }
                 }
-                if (zeroX) for (int j = 0; j < 5; ++j) F[j].x = 0.f;
-                if (zeroY) for (int j = 0; j < 5; ++j) F[j].y = 0.f;
                 // calcDerivFromFlux: x difference of (x, r) (its right face flux
                 // by shuffle), then the y difference of (x, r-1) added to its x
                 // difference, each fma(FL - FR, area, deriv) rounded as written
+                // (a face of no area has no flux)
                 float deriv[5];
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
-                    float const fx = F[f].x;
-                    float const fy = F[yFrameOf(f)].y;
+                    float const fx = zeroX ? 0.f : F[f].x;
+                    float const fy = zeroY ? 0.f : F[yFrameOf(f)].y;
                     float const fxr = __shfl_down_sync(FULL, fx, 1);
                     deriv[f] = skipY ? Dxp[f] : __fmaf_rn(__fsub_rn(Fyp[f], fy), ary, Dxp[f]);
                     Dxp[f] = skipX ? 0.f : __fmaf_rn(__fsub_rn(fx, fxr), arx, 0.f);

@@ -277,10 +277,8 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                 lanes::C5<float2> UL, UR;
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
-                    UL.u[j].x = __shfl_up_sync(FULL, R[j].x, 1);
-                    UR.u[j].x = L[j].x;
-                    UL.u[j].y = Ry[j];
-                    UR.u[j].y = L[j].y;
+                    UL.u[j] = make_float2(__shfl_up_sync(FULL, R[j].x, 1), Ry[j]);
+                    UR.u[j] = L[j];
                 }
                 float2 F[5];
                 bool const plain = lanes::roeUp2(F, le, UL, UR);

@@ -280,10 +280,8 @@ __global__ void __launch_bounds__(NWY * 32, OCC) k_march3(const __grid_constant_
                 lanes::C5<float2> UL, UR;
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
-                    UL.u[j].x = __shfl_up_sync(FULL, Rxz[j].x, 1);
-                    UR.u[j].x = Lxz[j].x;
-                    UL.u[j].y = Rz[j];
-                    UR.u[j].y = Lxz[j].y;
+                    UL.u[j] = make_float2(__shfl_up_sync(FULL, Rxz[j].x, 1), Rz[j]);
+                    UR.u[j] = Lxz[j];
                     Rz[j] = Rxz[j].y;   // the next plane's cell below
                 }
                 if (iz >= 2) {

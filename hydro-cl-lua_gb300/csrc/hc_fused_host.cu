@@ -649,12 +649,6 @@ static void* pinned_device_ptr(const void* host) {
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
-// n admissions from host states in one pass: the host side of each, then the
-// uploads of the slots' descriptors in runs of consecutive slots, then every
-// state set up by its own load launch, which reads a page-locked host buffer
-// in place and otherwise its own range of one staging buffer, all queued back
-// to back (no wait).  Stops at the first instance the host side refuses;
-// *n_done = the instances admitted.
 // Batched set-up (load) or gather passes over n instances: one launch per
 // grid dimension and kXferJobs instances; job j moves state buffer bufs[j] of
 // slots[j] from / to hosts[j].
@@ -739,6 +733,13 @@ static int setup_many(FusedSet* f, int done, const int* slots, const void* const
     return HC_OK;
 }
 
+// n admissions from host states, in chunks of one set-up launch's instances:
+// the host side of each, then the chunk's memory zeroed, its descriptors
+// uploaded in runs of consecutive slots and its states set up by batched
+// load launches (a page-locked host buffer read in place, any other through
+// its own range of one staging buffer), all queued back to back (no wait).
+// Stops at the first instance the host side refuses; *n_done = the instances
+// admitted.
 int fused_add_many(FusedSet* f, int n, const int* slots, const hc_solver_desc* descs, const void* const* hosts,
                    int layout, const double* t_end, const long long* max_steps, int stop_on_error, int* n_done) {
     *n_done = 0;
@@ -762,10 +763,10 @@ int fused_add_many(FusedSet* f, int n, const int* slots, const hc_solver_desc* d
     return r;
 }
 
-// n fetches in one pass: every slot's state gathered by its own launch,
-// straight into a page-locked host buffer, otherwise into its own range of one
-// staging buffer (the gathers back to back) and copied out from there (the
-// copies back to back); no wait.
+// n fetches in one pass: the slots' states gathered by batched launches (one
+// per grid dimension and kXferJobs slots), straight into a page-locked host
+// buffer, otherwise into the slot's own range of one staging buffer and
+// copied out from there (the copies back to back); no wait.
 int fused_get_state_many(FusedSet* f, int n, const int* slots, void* const* hosts, int layout) {
     if (layout < 0 || layout > 2) return fail(HC_ERR_INVALID, "layout");
     std::vector<void*> direct(n);

@@ -354,8 +354,9 @@ int hc_batch_admit_init(hc_batch* b, const hc_solver_desc* desc, const hc_init* 
 /* `count` hc_batch_admit calls in one: instance k from descs[k], cons[k],
  * t_end[k], max_steps[k], tags[k] (t_end, max_steps, tags may be NULL: +inf,
  * no limit, k), all in `layout`.  Every instance is checked first; the
- * descriptors of the accepted ones are uploaded together and their set-up
- * launches queued back to back and waited for once.  A buffer in page-locked
+ * descriptors of the accepted ones are uploaded together and their states set
+ * up by batched launches (one per grid dimension and 120 instances), queued
+ * back to back and waited for once.  A buffer in page-locked
  * host memory (hc_host_alloc, cudaHostRegister) is read in place by its
  * set-up kernel over the host link; other buffers go through a staging copy.
  * Stops at the first refusal or error and returns it; *n_admitted = the
@@ -391,9 +392,9 @@ int hc_batch_list(hc_batch* b, hc_done* out, int cap, int* n_out);
 /* Copies a slot's interior state to the host. */
 int hc_batch_fetch(hc_batch* b, int slot, void* cons, int layout);
 /* `count` hc_batch_fetch calls in one (slot slots[k] into cons[k], all in
- * `layout`), queued back to back and waited for once; a page-locked buffer is
- * written in place by its gather kernel.  Checks every slot before copying
- * anything. */
+ * `layout`): batched gather launches (one per grid dimension and 120 slots),
+ * queued back to back and waited for once; a page-locked buffer is written in
+ * place by the gather kernel.  Checks every slot before copying anything. */
 int hc_batch_fetch_many(hc_batch* b, int count, const int* slots, void* const* cons, int layout);
 /* Frees a slot and returns its bytes to the budget. */
 int hc_batch_retire(hc_batch* b, int slot);

@@ -4,13 +4,14 @@
 // lanes 0 and 31 carry the cells beside the strip) over a segment of seg
 // rows (H, the schedule's segment, unless the host shortens the segments of a
 // launch whose items would leave warps idle).
-// The warp marches up the segment one row per step.  Its lane's column of
-// cells passes through registers: the cell below, the cell and the cell above
-// (the last loaded from shared memory), the cell below's y-side R state and
-// y-face flux, and the row below's x-flux difference.  Each step of a lane:
-//   * the x and y half slopes of its cell (x neighbours from shared memory,
-//     y neighbours from registers), evaluated together on FP32 register pairs
-//     (.x: the x axis, .y: the y axis);
+// The warp marches up the segment one row per step.  The cells come from the
+// chunk buffers in shared memory (rows r-1 .. r+1 at every step); a lane
+// carries in registers the cell below's y-side R state and y-face flux and the
+// row below's x-flux difference.  Each step of a lane:
+//   * the x and y half slopes of its cell, evaluated together on FP32
+//     register pairs (.x: the x axis, .y: the y axis; pair j holds global
+//     field j on x and the y interface frame's field j on y, the order the
+//     Roe lanes take);
 //   * the Roe flux of its cell's left x face (the left neighbour's R state
 //     comes by warp shuffle) and of its cell's lower y face, together on
 //     register pairs;

@@ -387,17 +387,11 @@ __global__ void __launch_bounds__(NW * 32, OCC) k_march2(const __grid_constant__
                         }
                         if constexpr (EPI != 1) {
                             // the next row's cell (the segment's last row read
-                            // again at its end: no branch), and into L2 eight
-                            // rows ahead (the last row repeated near the end)
-                            const float* const pc = a0src + idx;
-                            const float* const pn = pc + (yc + 1 < y0 + rows ? geo.px : 0);
+                            // again at its end: no branch); issued a row ahead
+                            // of its use, it needs no L2 prefetch besides
+                            const float* const pn = a0src + idx + (yc + 1 < y0 + rows ? geo.px : 0);
 #pragma unroll
                             for (int f = 0; f < 5; ++f) pre[f] = pn[f * geo.plane];
-                            int const ahead = yc + 8 < y0 + rows ? 8 : y0 + rows - 1 - yc;
-                            const float* const pf = pc + (long long)ahead * geo.px;
-#pragma unroll
-                            for (int f = 0; f < 5; ++f)
-                                asm volatile("prefetch.global.L2 [%0];" ::"l"(pf + f * geo.plane));
                         }
 #pragma unroll
                         for (int f = 0; f < 5; ++f) u[f] = lanes::fma(deriv[f], cbcur, u[f]);
